@@ -1,0 +1,138 @@
+/*
+ * sparc_gb300.h -- C ABI of the GB300 wave-solver hot path (2-D displacement formulation
+ * with flows and PML, 5-stage low-storage Runge-Kutta, seismograms and kernel snapshots).
+ *
+ * Conventions
+ *   - Bulk arrays are DEVICE pointers owned by the caller (PyTorch tensors on the Python
+ *     side); the library never frees caller memory.  Small tables are host pointers.
+ *   - Every field is x-fastest: f[k*nx + i], k = 0 the deepest level (the Fortran layout
+ *     a(nx,ny,nz) of the reference with ny = 1); batch (solve) index outermost.
+ *   - Every function returns SPARC_OK (0) or a negative code and never throws; the message
+ *     of the last failure on the calling thread is sparc_last_error().
+ *   - One plan per host thread.  All work is queued on the stream given (cudaStream_t
+ *     passed as void*), nothing synchronises the device except where stated.
+ */
+#ifndef SPARC_GB300_H
+#define SPARC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPARC_OK 0
+#define SPARC_ERR_ARG (-1)         /* bad argument (null pointer, inconsistent sizes) */
+#define SPARC_ERR_SIZE (-2)        /* unsupported size (nx not in the FFT table, nz too small) */
+#define SPARC_ERR_NONFINITE (-3)   /* non-finite values found in the state */
+#define SPARC_ERR_TIMEOUT (-4)     /* a bounded device wait gave up */
+#define SPARC_ERR_CUDA (-5)        /* CUDA runtime error */
+#define SPARC_ERR_STATE (-6)       /* call out of order (e.g. run before background) */
+
+typedef struct sparc_plan sparc_plan_t;
+
+/* Grid, batch and run parameters.  Replaces the compile-time params.i (params.i:26-165) and
+ * the module globals set by Initialize_all / mp_Initialize_RHS_2d / INITIALIZE_STEP
+ * (initialize.f90:167-474, physics2d.f90:23-405, step.f90:24-41). */
+typedef struct {
+    int nx, nz, nbatch;        /* grid and number of independent solves in the batch */
+    int precision;             /* 32 (FP32 state and arithmetic) or 64 (FP64) */
+    int npmlbot, npmltop;      /* vertical PML layers (params.i:121) */
+    int npmlhor;               /* horizontal PML columns per side (params.i:91) */
+    double deltat;             /* nondimensional step timestep*dimc/diml (initialize.f90:474) */
+    double stretchx;           /* rsun/xlength (initialize.f90:225) */
+    double betas[5];           /* RK stage coefficients times deltat (step.f90:34-40) */
+    int flows;                 /* BACKGROUND_FLOWS_EXIST: advection terms on (params.i:70) */
+    int c2d;                   /* 1: c2rho0 is a 2-D (nz x nx) field, 0: a profile in z */
+    int bg_per_solve;          /* 1: 2-D background arrays are given per solve */
+    int steps_out;             /* record cadence in steps (driver.f90:209) */
+    int k_inj;                 /* 0-based injection row (e_rad forward, o_rad adjoint) */
+    int k_obs;                 /* 0-based observation row o_rad (physics2d.f90:43-50) */
+    int src_until;             /* inject while time <= src_until (physics2d.f90:1049) */
+} sparc_config_t;
+
+/* Background, all DEVICE pointers to FP64 arrays; copied (and rounded for FP32 plans) into
+ * the plan.  nbg = nbatch if bg_per_solve else 1; nzpml = npmlbot + npmltop;
+ * nhx = 2*npmlhor.  Mirrors the arrays of mp_Initialize_RHS_2d (physics2d.f90:226-357). */
+typedef struct {
+    const double *stretch, *unstretch;            /* [nz] (initialize.f90:466-470) */
+    const double *rhoinv, *rho0;                  /* [nz] */
+    const double *gradp0_z, *gradrho0_z;          /* [nz], before the PML decay factor */
+    const double *g;                              /* [nz], with the PML decay factor applied */
+    const double *fdz;                            /* [nbg][nzpml][nx] PML decay (functiondecay) */
+    const double *az, *bz;                        /* [nbg][nzpml][nx] vertical PML coefficients */
+    const double *ax, *bx;                        /* [nbg][nz][nhx] horizontal PML coefficients */
+    const double *c2rho0;                         /* [nbg][nz][nx] if c2d else [nz] */
+    const double *v0x, *v0z;                      /* [nbg][nz][nx] or NULL when flows == 0 */
+} sparc_background_t;
+
+/* Create / destroy.  Replaces the allocation and FFT planning of Initialize_all
+ * (initialize.f90:317-346) and the compact-FD matrix set-up of dbyd2.f:151-196. */
+int sparc_plan_create(const sparc_config_t *cfg, sparc_plan_t **plan);
+int sparc_plan_destroy(sparc_plan_t *plan);
+const char *sparc_last_error(void);
+
+/* Sixth-order compact z-derivative of n1 columns of nz values (FP64, device pointers):
+ * dvar = stretch .* dbyd2(var, ibc).  ibc 0..3 as dbyd2.f:19-24; for ibc 2 (3) the row-0
+ * (row nz-1) value is taken from preset[n1] (NULL means zero).  stretch NULL means 1.
+ * Replaces ddz (derivatives.f90:10-24) and DBYD2 (dbyd2.f:8-235). */
+int sparc_ddz(sparc_plan_t *plan, const double *var, double *dvar, int n1, int ibc,
+              const double *preset, const double *stretch, void *stream);
+
+/* Spectral x-derivative of nrows rows of nx values (FP64, device pointers), times stretchx.
+ * Replaces ddx (derivatives.f90:28-58). */
+int sparc_ddx(sparc_plan_t *plan, const double *var, double *dvar, int nrows, double stretchx,
+              void *stream);
+
+/* Upload the background (see sparc_background_t). */
+int sparc_set_background(sparc_plan_t *plan, const sparc_background_t *bg, void *stream);
+
+/* Sources (DEVICE pointers, FP64).  The forcing added to RHS v_z at row k_inj at step t is
+ *   inj_scale[b][x] * sum_j wts[t][j] * rows[b][idx[t]+j][x],  j = 0..6,
+ * rows beyond nrows count as zero.  This covers the forward source vr(x)*fwdsource(t+1)
+ * (physics2d.f90:1056-1058, nrows = 1, wts[t][0] = fwdsource(t+1)) and the 7-point
+ * Lagrange-interpolated adjoint source (physics.f90:678-737, physics2d.f90:1052-1054).
+ * inj_scale = delta_width / rho0(x, k_inj).  wts: [ntab][7], idx: [ntab] (host pointers). */
+int sparc_set_source(sparc_plan_t *plan, const double *inj_scale, const double *rows, int nrows,
+                     const double *wts, const int *idx, int ntab, void *stream);
+
+/* Zero the state, PML auxiliaries and RHS registers and set the step counter to time0. */
+int sparc_reset_state(sparc_plan_t *plan, int time0, void *stream);
+
+/* Advance every solve of the batch by nsteps steps of STEP (step.f90:43-119) inside
+ * TIMESTEPPING (driver.f90:351-456).  flow_sign multiplies v0 (+1 forward, -1 for the
+ * reference adjoint, driver.f90:144-147).  After each step whose counter is a multiple of
+ * steps_out the record a(:,k_obs,v_z) is written to seis (DEVICE, plan precision,
+ * [nbatch][nrec_cap][nx]) at index time/steps_out; if snaps is not NULL the partial state of
+ * all_modules.f90:750-784 (xi_x, xi_z, v_x, v_z, acc_x, acc_z) goes to snaps
+ * ([nbatch][nrec_cap][6][nz][nx]).  Records past nrec_cap are dropped.  use_graph != 0
+ * captures one step in a CUDA graph and replays it. */
+int sparc_forward(sparc_plan_t *plan, int nsteps, double flow_sign, void *seis, void *snaps,
+                  int nrec_cap, int use_graph, void *stream);
+
+/* The state of solve b: copy the four live fields (xi_x, xi_z, v_x, v_z), each nz*nx of the
+ * plan precision, to or from DEVICE memory (for checkpoints and tests). */
+int sparc_get_state(sparc_plan_t *plan, void *dst, void *stream);
+int sparc_set_state(sparc_plan_t *plan, const void *src, void *stream);
+
+/* Current step counter (synchronises the stream). */
+int sparc_get_time(sparc_plan_t *plan, int *time, void *stream);
+
+/* Kernel construction from paired snapshots (kernels.f90:209-358): for record pair
+ * (j, jadj = nadj-1-j), j = 0..npair-1, accumulate in FP64
+ *   kc  += div(f_xi) * div(a_v),  kvx += d_x(f_v) . a_v,  kvz += d_z(f_v) . a_v,
+ *   hes += |f_acc|^2
+ * with d_z filtered by FILTER_VAR_Z (kernels.f90:891-928).  fsn / asn are DEVICE snapshot
+ * arrays of the plan precision as written by sparc_forward ([nbatch][nrec][6][nz][nx]);
+ * out is DEVICE FP64 [nbatch][4][nz][nx] (kc, kvx, kvz, hes), accumulated into. */
+int sparc_kernels(sparc_plan_t *plan, const void *fsn, int nfwd, const void *asn, int nadj,
+                  int npair, double *out, void *stream);
+
+/* Host-only FP64 evaluation of the partitioned compact-derivative algebra that the device
+ * code applies (no GPU needed): x[nz][n1] = dbyd2(b, ibc) without the stretch factor, with
+ * the same chunking as a plan whose chunks hold at most lmax rows.  For validating the
+ * precomputed tables against dbyd2.f (dbyd2.f:8-235). */
+int sparc_zsolve_host(int nz, int ibc, int lmax, const double *b, double *x, const double *preset, int n1);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPARC_GB300_H */

@@ -284,7 +284,8 @@ def np_ddx(f, stretchx):
     F = F * (1j * kap)
     if nx % 2 == 0:
         F[..., -1] = 0.0
-    return np.fft.irfft(F, n=nx, axis=-1) * stretchx
+    # FFTW's c2r is unnormalised (the 1/nx sits in eyekx); numpy's irfft divides by nx
+    return np.fft.irfft(F, n=nx, axis=-1) * nx * stretchx
 
 
 FILTER_COEFFS = np.array([0.75390625, 0.41015625, -0.234375, 0.087890625, -0.01953125, 0.001953125])

@@ -1,0 +1,83 @@
+"""ctypes binding of the C ABI in include/sparc_gb300.h (libsparc_gb300.so).
+
+The library is the only compute path: if it cannot be loaded the import of the solver
+fails loudly (there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import _build
+
+_LIB = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_vp = ctypes.c_void_p
+
+SPARC_OK = 0
+ERRORS = {-1: "bad argument", -2: "unsupported size", -3: "non-finite state", -4: "device wait timed out",
+          -5: "CUDA error", -6: "call out of order"}
+
+# Every function declared in include/sparc_gb300.h, with its ctypes signature.
+SIGNATURES = {
+    "sparc_plan_create": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "sparc_plan_destroy": (ctypes.c_int, [_vp]),
+    "sparc_last_error": (ctypes.c_char_p, []),
+    "sparc_ddz": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    "sparc_ddx": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_double, _vp]),
+    "sparc_set_background": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc_set_source": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _dp, _ip, ctypes.c_int, _vp]),
+    "sparc_reset_state": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "sparc_forward": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "sparc_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc_set_state": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc_get_time": (ctypes.c_int, [_vp, _ip, _vp]),
+    "sparc_kernels": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
+    "sparc_zsolve_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int]),
+}
+
+
+class SparcConfig(ctypes.Structure):
+    """sparc_config_t."""
+
+    _fields_ = [
+        ("nx", ctypes.c_int), ("nz", ctypes.c_int), ("nbatch", ctypes.c_int), ("precision", ctypes.c_int),
+        ("npmlbot", ctypes.c_int), ("npmltop", ctypes.c_int), ("npmlhor", ctypes.c_int),
+        ("deltat", ctypes.c_double), ("stretchx", ctypes.c_double), ("betas", ctypes.c_double * 5),
+        ("flows", ctypes.c_int), ("c2d", ctypes.c_int), ("bg_per_solve", ctypes.c_int),
+        ("steps_out", ctypes.c_int), ("k_inj", ctypes.c_int), ("k_obs", ctypes.c_int), ("src_until", ctypes.c_int),
+    ]
+
+
+class SparcBackground(ctypes.Structure):
+    """sparc_background_t (device pointers)."""
+
+    _fields_ = [(n, _vp) for n in ("stretch", "unstretch", "rhoinv", "rho0", "gradp0_z", "gradrho0_z", "g", "fdz",
+                                    "az", "bz", "ax", "bx", "c2rho0", "v0x", "v0z")]
+
+
+class SparcError(RuntimeError):
+    pass
+
+
+def lib(build: bool = True):
+    """Load (building first if sources changed) libsparc_gb300.so."""
+    global _LIB
+    if _LIB is None:
+        path = _build.build() if build else _build.LIB_PATH
+        if not os.path.exists(path):
+            raise SparcError(f"CUDA extension missing: {path}")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def check(rc: int, what: str):
+    if rc != SPARC_OK:
+        msg = lib().sparc_last_error()
+        raise SparcError(f"{what} failed ({ERRORS.get(rc, rc)}): {msg.decode() if msg else ''}")

@@ -1,0 +1,721 @@
+// sparc_capi.cu -- the C ABI of include/sparc_gb300.h: plan life cycle, FP64 construction of
+// the compact-derivative and FFT tables, background/source upload, and the step sequence
+//   R(1) C(1) R(2) C(2) ... R(5) C(5) R(6) E
+// (row pass, column pass of each RK stage, closing row pass, end-of-step update), captured in
+// a CUDA graph and replayed once per step.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "sparc_common.cuh"
+#include "sparc_gb300.h"
+
+using namespace sparc;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(SPARC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------------
+// Compact-derivative tables (FP64).  Coefficients follow dbyd2.f, where d2i, C1..C5, alpha,
+// alpha2, gamma2, alpha1, beta1, const and up1 are implicitly REAL(4): they are formed in float
+// and used as double.
+// ---------------------------------------------------------------------------------------------
+struct HostZTab {
+    int nz = 0, ibc = 0, nch = 0, L = 0, preset_row = -1;
+    double c1 = 0, c2 = 0;
+    std::vector<double> w5, ib, lwib, gm, WL, VU, G;
+    std::vector<double> lowr, uppr;
+};
+
+bool invert(std::vector<double> &M, int n)  // Gauss-Jordan with partial pivoting, in place
+{
+    std::vector<double> I(n * n, 0.0);
+    for (int i = 0; i < n; i++) I[i * n + i] = 1.0;
+    for (int col = 0; col < n; col++) {
+        int piv = col;
+        for (int r = col + 1; r < n; r++)
+            if (std::fabs(M[r * n + col]) > std::fabs(M[piv * n + col])) piv = r;
+        if (M[piv * n + col] == 0.0) return false;
+        if (piv != col)
+            for (int c = 0; c < n; c++) {
+                std::swap(M[piv * n + c], M[col * n + c]);
+                std::swap(I[piv * n + c], I[col * n + c]);
+            }
+        double d = M[col * n + col];
+        for (int c = 0; c < n; c++) { M[col * n + c] /= d; I[col * n + c] /= d; }
+        for (int r = 0; r < n; r++) {
+            if (r == col) continue;
+            double f = M[r * n + col];
+            if (f == 0.0) continue;
+            for (int c = 0; c < n; c++) { M[r * n + c] -= f * M[col * n + c]; I[r * n + c] -= f * I[col * n + c]; }
+        }
+    }
+    M = I;
+    return true;
+}
+
+bool chunking(int nz, int lmax, int &nch, int &L)
+{
+    nch = (nz + lmax - 1) / lmax;
+    L = (nz + nch - 1) / nch;
+    if (nch > (lmax >= 32 ? 12 : 20)) return false;  // block geometry of sparc_col.cu
+    return nz - (nch - 1) * L >= 2 && L >= 2;
+}
+
+bool build_ztab(int nz, int ibc, int nch, int L, HostZTab &t)
+{
+    if (nz < 8) return false;
+    t.nz = nz; t.ibc = ibc; t.nch = nch; t.L = L;
+    const float d2i = (float)(nz - 1);
+    const float C1 = d2i * 7.0f / 9.0f, C2 = d2i / 36.0f;  // dbyd2.f:82-83
+    t.c1 = C1; t.c2 = C2;
+    const float b1 = -(43.0f / 96.0f * d2i), b2 = -(5.0f / 6.0f * d2i), b3 = 9.0f / 8.0f * d2i,
+                b4 = 1.0f / 6.0f * d2i, b5 = -(1.0f / 96.0f * d2i);        // dbyd2.f:101-105
+    const float f1 = -(10.0f / 3.0f * d2i), f2 = -(3.0f * d2i), f3 = 6.0f * d2i, f4 = 1.0f / 3.0f * d2i;  // :119-122
+    const float alpha = 1.0f / 3.0f, alpha2 = 3.0f / 4.0f, gamma2 = 1.0f / 8.0f, alpha1 = 6.0f, beta1 = 3.0f;
+    const float cnst = 1.0f / (alpha2 - beta1 * gamma2);
+    const float up1 = (alpha1 * alpha2 - beta1) * cnst;
+    t.w5.assign((size_t)nz * 5, 0.0);
+    const double r1[5] = {b1, b2, b3, b4, b5};                 // row 1 on b[0..4]
+    const double rm2[5] = {-(double)b5, -(double)b4, -(double)b3, -(double)b2, -(double)b1};  // row nz-2 on b[nz-5..]
+    for (int j = 0; j < 5; j++) { t.w5[1 * 5 + j] = r1[j]; t.w5[(size_t)(nz - 2) * 5 + j] = rm2[j]; }
+    t.preset_row = -1;
+    if (ibc == 1 || ibc == 3) {  // row 0: 4-point closure, then preconditioned with row 1 (dbyd2.f:178-182)
+        const double r0[5] = {f1, f2, f3, f4, 0.0};
+        for (int j = 0; j < 5; j++) t.w5[j] = ((double)alpha2 * r0[j] - (double)beta1 * r1[j]) * (double)cnst;
+    }
+    if (ibc == 1 || ibc == 2) {  // row nz-1 on b[nz-5..nz-1] (dbyd2.f:139-142, 183-187)
+        const double rl[5] = {0.0, -(double)f4, -(double)f3, -(double)f2, -(double)f1};
+        for (int j = 0; j < 5; j++)
+            t.w5[(size_t)(nz - 1) * 5 + j] = ((double)alpha2 * rl[j] - (double)beta1 * rm2[j]) * (double)cnst;
+    }
+    if (ibc == 2) t.preset_row = 0;
+    if (ibc == 3) t.preset_row = nz - 1;
+    // matrix (dbyd2.f:151-196)
+    t.uppr.assign(nz, 0.0);
+    t.lowr.assign(nz, 0.0);
+    for (int k = 2; k <= nz - 3; k++) t.uppr[k] = alpha;
+    t.uppr[0] = (ibc % 2 == 0) ? 0.0 : (double)up1;
+    t.uppr[1] = alpha2;
+    t.uppr[nz - 2] = gamma2;
+    for (int k = 0; k < nz; k++) t.lowr[k] = t.uppr[nz - 1 - k];
+    t.lowr[nz - 1] = (ibc != 1 && ibc != 2) ? 0.0 : (double)up1;
+    t.uppr[nz - 1] = 0.0;
+    t.lowr[0] = 0.0;
+    // chunk-local factors and spikes
+    t.ib.assign(nz, 0.0); t.lwib.assign(nz, 0.0); t.gm.assign(nz, 0.0);
+    t.WL.assign(nz, 0.0); t.VU.assign(nz, 0.0);
+    std::vector<double> bet(nz), w(nz), v(nz);
+    for (int c = 0; c < nch; c++) {
+        const int s = c * L, e = std::min(nz, (c + 1) * L) - 1;
+        bet[s] = 1.0;
+        t.ib[s] = 1.0;
+        for (int k = s + 1; k <= e; k++) {
+            t.gm[k] = t.uppr[k - 1] / bet[k - 1];
+            bet[k] = 1.0 - t.lowr[k] * t.gm[k];
+            t.ib[k] = 1.0 / bet[k];
+            t.lwib[k] = t.lowr[k] * t.ib[k];
+        }
+        auto solve = [&](std::vector<double> &y, int unit_row) {
+            for (int k = s; k <= e; k++) {
+                double r = (k == unit_row) ? 1.0 : 0.0;
+                y[k] = r * t.ib[k] - (k > s ? t.lwib[k] * y[k - 1] : 0.0);
+            }
+            for (int k = e - 1; k >= s; k--) y[k] -= t.gm[k + 1] * y[k + 1];
+        };
+        solve(w, s);
+        solve(v, e);
+        const double ls = (s > 0) ? t.lowr[s] : 0.0;
+        const double ue = (e < nz - 1) ? t.uppr[e] : 0.0;
+        for (int k = s; k <= e; k++) { t.WL[k] = ls * w[k]; t.VU[k] = ue * v[k]; }
+    }
+    // reduced system for u = (x[s_0], x[e_0], x[s_1], x[e_1], ...)
+    const int n2 = 2 * nch;
+    std::vector<double> M((size_t)n2 * n2, 0.0);
+    for (int c = 0; c < nch; c++) {
+        const int s = c * L, e = std::min(nz, (c + 1) * L) - 1;
+        const int rows[2] = {s, e};
+        for (int h = 0; h < 2; h++) {
+            const int r = 2 * c + h, k = rows[h];
+            M[(size_t)r * n2 + r] += 1.0;
+            if (c > 0) M[(size_t)r * n2 + (2 * c - 1)] += t.WL[k];
+            if (c < nch - 1) M[(size_t)r * n2 + (2 * c + 2)] += t.VU[k];
+        }
+    }
+    if (!invert(M, n2)) return false;
+    t.G = M;
+    return true;
+}
+
+// Host evaluation of the partitioned solve (same algebra as the device code).
+void zsolve_host(const HostZTab &t, const double *b, double *x, const double *preset_v, int n1)
+{
+    const int nz = t.nz, nch = t.nch, L = t.L, n2 = 2 * nch;
+    std::vector<double> col(nz), y(nz), ub(n2);
+    for (int i = 0; i < n1; i++) {
+        for (int k = 0; k < nz; k++) col[k] = b[(size_t)k * n1 + i];
+        auto rhs = [&](int k) {
+            if (k >= 2 && k <= nz - 3) return t.c1 * (col[k + 1] - col[k - 1]) + t.c2 * (col[k + 2] - col[k - 2]);
+            if (k == t.preset_row) return preset_v ? preset_v[i] : 0.0;
+            const int base = (k <= 1) ? 0 : nz - 5;
+            double r = 0.0;
+            for (int j = 0; j < 5; j++) r += t.w5[(size_t)k * 5 + j] * col[base + j];
+            return r;
+        };
+        for (int c = 0; c < nch; c++) {
+            const int s = c * L, e = std::min(nz, (c + 1) * L) - 1;
+            for (int k = s; k <= e; k++) y[k] = rhs(k) * t.ib[k] - (k > s ? t.lwib[k] * y[k - 1] : 0.0);
+            for (int k = e - 1; k >= s; k--) y[k] -= t.gm[k + 1] * y[k + 1];
+            ub[2 * c] = y[s];
+            ub[2 * c + 1] = y[e];
+        }
+        for (int c = 0; c < nch; c++) {
+            const int s = c * L, e = std::min(nz, (c + 1) * L) - 1;
+            double xl = 0, xr = 0;
+            if (c > 0) for (int q = 0; q < n2; q++) xl += t.G[(size_t)(2 * c - 1) * n2 + q] * ub[q];
+            if (c < nch - 1) for (int q = 0; q < n2; q++) xr += t.G[(size_t)(2 * c + 2) * n2 + q] * ub[q];
+            for (int k = s; k <= e; k++) x[(size_t)k * n1 + i] = y[k] - t.WL[k] * xl - t.VU[k] * xr;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Device memory helpers
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void cast_kernel(const double *__restrict__ src, T *__restrict__ dst, size_t n)
+{
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) dst[i] = (T)src[i];
+}
+
+template <typename T>
+cudaError_t cast_to(const double *src, T *dst, size_t n, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 4096);
+    cast_kernel<T><<<blocks, 256, 0, st>>>(src, dst, n);
+    return cudaGetLastError();
+}
+
+template <typename T>
+struct DevZ {
+    T *buf = nullptr;
+    ZTab<T> tab{};
+};
+
+template <typename T>
+cudaError_t upload_ztab(const HostZTab &h, DevZ<T> &d, std::vector<void *> &allocs)
+{
+    const int nz = h.nz, n2 = 2 * h.nch;
+    const size_t n = (size_t)nz * 5 + (size_t)nz * 5 + (size_t)n2 * n2;
+    std::vector<T> host(n);
+    size_t o = 0;
+    auto put = [&](const std::vector<double> &v) { for (double x : v) host[o++] = (T)x; };
+    put(h.w5); put(h.ib); put(h.lwib); put(h.gm); put(h.WL); put(h.VU); put(h.G);
+    cudaError_t e = cudaMalloc(&d.buf, n * sizeof(T));
+    if (e != cudaSuccess) return e;
+    allocs.push_back(d.buf);
+    e = cudaMemcpy(d.buf, host.data(), n * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    T *p = d.buf;
+    d.tab.w5 = p; p += (size_t)nz * 5;
+    d.tab.ib = p; p += nz;
+    d.tab.lwib = p; p += nz;
+    d.tab.gm = p; p += nz;
+    d.tab.WL = p; p += nz;
+    d.tab.VU = p; p += nz;
+    d.tab.G = p;
+    d.tab.c1 = (T)h.c1;
+    d.tab.c2 = (T)h.c2;
+    d.tab.preset_row = h.preset_row;
+    return cudaSuccess;
+}
+
+template <typename T>
+struct DevFFT {
+    T *buf = nullptr;
+    const T *twr = nullptr, *twi = nullptr, *kap = nullptr;
+};
+
+template <typename T>
+cudaError_t upload_fft(int n, DevFFT<T> &d, std::vector<void *> &allocs)
+{
+    std::vector<T> host((size_t)3 * n);
+    const double pi = 3.141592653589793;
+    for (int t = 0; t < n; t++) {
+        host[t] = (T)std::cos(2.0 * pi * (double)t / (double)n);
+        host[n + t] = (T)(-std::sin(2.0 * pi * (double)t / (double)n));
+        double kap;  // eyekx (initialize.f90:206-208) with the Nyquist bin dropped by c2r
+        if (2 * t < n) kap = (double)t * (1.0 / (double)n) * 2.0 * pi;
+        else if (2 * t == n) kap = 0.0;
+        else kap = -(double)(n - t) * (1.0 / (double)n) * 2.0 * pi;
+        host[2 * n + t] = (T)kap;
+    }
+    cudaError_t e = cudaMalloc(&d.buf, host.size() * sizeof(T));
+    if (e != cudaSuccess) return e;
+    allocs.push_back(d.buf);
+    e = cudaMemcpy(d.buf, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice);
+    d.twr = d.buf; d.twi = d.buf + n; d.kap = d.buf + 2 * n;
+    return e;
+}
+
+template <typename T>
+struct Solver {
+    StepArgs<T> a{};
+    DevZ<T> z[4];
+    DevFFT<T> fft;
+    std::vector<void *> allocs;
+    size_t F = 0;
+    T *work = nullptr;  // kernel-accumulation scratch [nb][8][nz][nx]
+};
+
+}  // namespace
+
+struct sparc_plan {
+    sparc_config_t cfg{};
+    int nch = 0, L = 0, nch64 = 0, L64 = 0;
+    std::vector<void *> allocs;
+    HostZTab hz[4], hz64[4];
+    DevZ<double> z64[4];
+    DevFFT<double> fft64;
+    Solver<float> s32;
+    Solver<double> s64;
+    int *d_time = nullptr;
+    bool have_bg = false, have_src = false;
+    double unstretch_top = 1.0;
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    const void *g_seis = nullptr, *g_snaps = nullptr;
+    int g_cap = -1;
+    double g_fsign = 0.0;
+    cudaStream_t g_stream = nullptr;
+    double *d_srcw = nullptr;
+    int *d_srcidx = nullptr;
+};
+
+namespace {
+
+template <typename T>
+Solver<T> &solver(sparc_plan *p);
+template <>
+Solver<float> &solver<float>(sparc_plan *p) { return p->s32; }
+template <>
+Solver<double> &solver<double>(sparc_plan *p) { return p->s64; }
+
+template <typename T>
+int alloc_solver(sparc_plan *p)
+{
+    Solver<T> &S = solver<T>(p);
+    const sparc_config_t &c = p->cfg;
+    const int nx = c.nx, nz = c.nz, nb = c.nbatch;
+    const int nzpml = c.npmlbot + c.npmltop, nhx = 2 * c.npmlhor;
+    const size_t F = (size_t)nx * nz;
+    S.F = F;
+    const int nbg = c.bg_per_solve ? nb : 1;
+    struct Req { T **ptr; size_t n; };
+    T *A, *SV, *P, *RVXP, *DX, *FXX, *FXZ, *TOPDX, *PZ, *SPZ, *PX, *SPX;
+    T *rhoinv, *rho0, *gp0, *gr0, *g, *stretch, *fdz, *az, *bz, *ax, *bx, *c2rho0, *v0x, *v0z, *inj, *rows;
+    std::vector<Req> reqs = {
+        {&A, (size_t)nb * 4 * F}, {&SV, (size_t)3 * nb * 2 * F}, {&P, nb * F}, {&RVXP, nb * F}, {&DX, nb * F},
+        {&FXX, nb * F}, {&FXZ, nb * F}, {&TOPDX, (size_t)nb * nx},
+        {&PZ, (size_t)nb * 2 * nzpml * nx}, {&SPZ, (size_t)3 * nb * 2 * nzpml * nx},
+        {&PX, (size_t)nb * 2 * nz * nhx}, {&SPX, (size_t)3 * nb * 2 * nz * nhx},
+        {&rhoinv, (size_t)nz}, {&rho0, (size_t)nz}, {&gp0, (size_t)nz}, {&gr0, (size_t)nz}, {&g, (size_t)nz},
+        {&stretch, (size_t)nz}, {&fdz, (size_t)nbg * nzpml * nx}, {&az, (size_t)nbg * nzpml * nx},
+        {&bz, (size_t)nbg * nzpml * nx}, {&ax, (size_t)nbg * nz * nhx}, {&bx, (size_t)nbg * nz * nhx},
+        {&c2rho0, c.c2d ? nbg * F : (size_t)nz}, {&v0x, c.flows ? nbg * F : 1}, {&v0z, c.flows ? nbg * F : 1},
+        {&inj, (size_t)nb * nx}, {&rows, (size_t)nb * nx},
+    };
+    for (auto &r : reqs) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(r.n, 1) * sizeof(T));
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        S.allocs.push_back(ptr);
+        cudaMemset(ptr, 0, std::max<size_t>(r.n, 1) * sizeof(T));
+        *r.ptr = (T *)ptr;
+    }
+    // tables
+    for (int ibc = 0; ibc < 4; ibc++) {
+        cudaError_t e = upload_ztab<T>(p->hz[ibc], S.z[ibc], S.allocs);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("table upload: ") + cudaGetErrorString(e));
+    }
+    {
+        cudaError_t e = upload_fft<T>(nx, S.fft, S.allocs);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("fft upload: ") + cudaGetErrorString(e));
+    }
+    StepArgs<T> &a = S.a;
+    a.nx = nx; a.nz = nz; a.nb = nb; a.nh = c.npmlhor; a.nhx = nhx; a.nzpml = nzpml;
+    a.npmlbot = c.npmlbot; a.npmltop = c.npmltop;
+    a.flows = c.flows; a.c2d = c.c2d;
+    a.bg2 = c.bg_per_solve ? (long long)F : 0;
+    a.bgz = c.bg_per_solve ? (long long)nzpml * nx : 0;
+    a.bgx = c.bg_per_solve ? (long long)nz * nhx : 0;
+    a.dt = (T)c.deltat; a.stretchx = (T)c.stretchx; a.fsign = T(1);
+    a.A = A; a.SV = SV; a.P = P; a.RVXP = RVXP; a.DX = DX; a.FXX = FXX; a.FXZ = FXZ; a.TOPDX = TOPDX;
+    a.PZ = PZ; a.SPZ = SPZ; a.PX = PX; a.SPX = SPX;
+    a.rhoinv = rhoinv; a.rho0 = rho0; a.gp0 = gp0; a.gr0 = gr0; a.g = g; a.stretch = stretch;
+    a.fdz = fdz; a.az = az; a.bz = bz; a.ax = ax; a.bx = bx; a.c2rho0 = c2rho0; a.v0x = v0x; a.v0z = v0z;
+    a.twr = S.fft.twr; a.twi = S.fft.twi; a.kap = S.fft.kap;
+    a.z1 = S.z[1].tab; a.z2 = S.z[2].tab; a.z3 = S.z[3].tab;
+    a.nch = p->nch; a.L = p->L;
+    a.d_time = p->d_time;
+    a.src_until = c.src_until; a.k_inj = c.k_inj; a.k_obs = c.k_obs; a.steps_out = c.steps_out;
+    a.inj_scale = inj; a.src_rows = rows; a.nrows = 1;
+    return SPARC_OK;
+}
+
+template <typename T>
+void free_solver(Solver<T> &S)
+{
+    for (void *q : S.allocs) cudaFree(q);
+    S.allocs.clear();
+}
+
+template <typename T>
+cudaError_t enqueue_step(sparc_plan *p, StepArgs<T> a, cudaStream_t st)
+{
+    const double *B = p->cfg.betas;  // B[s-1] = beta of stage s (B[0] = 0)
+    cudaError_t e;
+    for (int s = 1; s <= 5; s++) {
+        a.stage = s;
+        a.bs = (T)B[s - 1];
+        a.bsm1 = (s >= 2) ? (T)B[s - 2] : T(0);
+        a.slot_s = s % 3; a.slot_sm1 = (s - 1) % 3; a.slot_sm2 = (s + 1) % 3;  // (s-2) mod 3
+        if ((e = launch_row_stage<T>(a, st)) != cudaSuccess) return e;
+        if ((e = launch_col_stage<T>(a, st)) != cudaSuccess) return e;
+    }
+    a.stage = 6;
+    a.bs = (T)0; a.bsm1 = (T)B[4];
+    a.slot_s = 0; a.slot_sm1 = 5 % 3; a.slot_sm2 = 4 % 3;
+    if ((e = launch_row_stage<T>(a, st)) != cudaSuccess) return e;
+    a.stage = 7;
+    a.bs = (T)B[4];
+    a.slot_s = 5 % 3; a.slot_sm1 = 4 % 3;
+    return launch_end_step<T>(a, st);
+}
+
+template <typename T>
+int run_forward(sparc_plan *p, int nsteps, double fsign, void *seis, void *snaps, int cap, int use_graph,
+                cudaStream_t st)
+{
+    Solver<T> &S = solver<T>(p);
+    StepArgs<T> a = S.a;
+    a.fsign = (T)fsign;
+    a.seis = (T *)seis;
+    a.snaps = (T *)snaps;
+    a.nrec_cap = cap;
+    a.unstretch_top = (T)p->unstretch_top;
+    if (!use_graph) {
+        for (int i = 0; i < nsteps; i++) CK(enqueue_step<T>(p, a, st));
+        return SPARC_OK;
+    }
+    const bool same = p->gexec && p->g_seis == seis && p->g_snaps == snaps && p->g_cap == cap &&
+                      p->g_fsign == fsign && p->g_stream == st;
+    if (!same) {
+        if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
+        if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+        // warm the launch attributes outside of capture
+        cudaStream_t cap_st;
+        CK(cudaStreamCreateWithFlags(&cap_st, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) e = enqueue_step<T>(p, a, cap_st);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(cap_st, &g);
+        cudaStreamDestroy(cap_st);
+        if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return fail(SPARC_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e)); }
+        if (e2 != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
+        p->graph = g;
+        CK(cudaGraphInstantiate(&p->gexec, g, 0));
+        p->g_seis = seis; p->g_snaps = snaps; p->g_cap = cap; p->g_fsign = fsign; p->g_stream = st;
+    }
+    for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(p->gexec, st));
+    return SPARC_OK;
+}
+
+template <typename T>
+int set_background(sparc_plan *p, const sparc_background_t *bg, cudaStream_t st)
+{
+    Solver<T> &S = solver<T>(p);
+    StepArgs<T> &a = S.a;
+    const sparc_config_t &c = p->cfg;
+    const int nz = c.nz, nx = c.nx, nzpml = c.npmlbot + c.npmltop, nhx = 2 * c.npmlhor;
+    const int nbg = c.bg_per_solve ? c.nbatch : 1;
+    if (!bg->stretch || !bg->unstretch || !bg->rhoinv || !bg->rho0 || !bg->gradp0_z || !bg->gradrho0_z || !bg->g ||
+        !bg->fdz || !bg->az || !bg->bz || !bg->ax || !bg->bx || !bg->c2rho0)
+        return fail(SPARC_ERR_ARG, "sparc_set_background: missing array");
+    if (c.flows && (!bg->v0x || !bg->v0z)) return fail(SPARC_ERR_ARG, "sparc_set_background: flows need v0x, v0z");
+    CK(cast_to<T>(bg->stretch, (T *)a.stretch, nz, st));
+    CK(cast_to<T>(bg->rhoinv, (T *)a.rhoinv, nz, st));
+    CK(cast_to<T>(bg->rho0, (T *)a.rho0, nz, st));
+    CK(cast_to<T>(bg->gradp0_z, (T *)a.gp0, nz, st));
+    CK(cast_to<T>(bg->gradrho0_z, (T *)a.gr0, nz, st));
+    CK(cast_to<T>(bg->g, (T *)a.g, nz, st));
+    CK(cast_to<T>(bg->fdz, (T *)a.fdz, (size_t)nbg * nzpml * nx, st));
+    CK(cast_to<T>(bg->az, (T *)a.az, (size_t)nbg * nzpml * nx, st));
+    CK(cast_to<T>(bg->bz, (T *)a.bz, (size_t)nbg * nzpml * nx, st));
+    CK(cast_to<T>(bg->ax, (T *)a.ax, (size_t)nbg * nz * nhx, st));
+    CK(cast_to<T>(bg->bx, (T *)a.bx, (size_t)nbg * nz * nhx, st));
+    CK(cast_to<T>(bg->c2rho0, (T *)a.c2rho0, c.c2d ? (size_t)nbg * nz * nx : (size_t)nz, st));
+    if (c.flows) {
+        CK(cast_to<T>(bg->v0x, (T *)a.v0x, (size_t)nbg * nz * nx, st));
+        CK(cast_to<T>(bg->v0z, (T *)a.v0z, (size_t)nbg * nz * nx, st));
+    }
+    double ut = 0.0;
+    CK(cudaMemcpyAsync(&ut, bg->unstretch + (nz - 1), sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    p->unstretch_top = ut;
+    p->have_bg = true;
+    return SPARC_OK;
+}
+
+template <typename T>
+int set_source(sparc_plan *p, const double *inj, const double *rows, int nrows, const double *wts, const int *idx,
+               int ntab, cudaStream_t st)
+{
+    Solver<T> &S = solver<T>(p);
+    StepArgs<T> &a = S.a;
+    const int nb = p->cfg.nbatch, nx = p->cfg.nx;
+    if (nrows > a.nrows) {
+        void *ptr = nullptr;
+        CK(cudaMalloc(&ptr, (size_t)nb * nrows * nx * sizeof(T)));
+        S.allocs.push_back(ptr);
+        a.src_rows = (const T *)ptr;
+    }
+    a.nrows = nrows;
+    CK(cast_to<T>(inj, (T *)a.inj_scale, (size_t)nb * nx, st));
+    CK(cast_to<T>(rows, (T *)a.src_rows, (size_t)nb * nrows * nx, st));
+    if (p->d_srcw) { cudaFree(p->d_srcw); p->d_srcw = nullptr; }
+    if (p->d_srcidx) { cudaFree(p->d_srcidx); p->d_srcidx = nullptr; }
+    CK(cudaMalloc(&p->d_srcw, (size_t)std::max(ntab, 1) * 7 * sizeof(double)));
+    CK(cudaMalloc(&p->d_srcidx, (size_t)std::max(ntab, 1) * sizeof(int)));
+    CK(cudaMemcpyAsync(p->d_srcw, wts, (size_t)ntab * 7 * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p->d_srcidx, idx, (size_t)ntab * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    a.src_w = p->d_srcw;
+    a.src_idx = p->d_srcidx;
+    a.ntab = ntab;
+    p->have_src = true;
+    // a new source invalidates a captured graph (its arguments changed)
+    if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    return SPARC_OK;
+}
+
+template <typename T>
+int reset_state(sparc_plan *p, int time0, cudaStream_t st)
+{
+    Solver<T> &S = solver<T>(p);
+    StepArgs<T> &a = S.a;
+    const sparc_config_t &c = p->cfg;
+    const size_t F = S.F;
+    const int nb = c.nbatch, nzpml = c.npmlbot + c.npmltop, nhx = 2 * c.npmlhor;
+    CK(cudaMemsetAsync(a.A, 0, (size_t)nb * 4 * F * sizeof(T), st));
+    CK(cudaMemsetAsync(a.SV, 0, (size_t)3 * nb * 2 * F * sizeof(T), st));
+    CK(cudaMemsetAsync(a.PZ, 0, (size_t)nb * 2 * nzpml * c.nx * sizeof(T), st));
+    CK(cudaMemsetAsync(a.SPZ, 0, (size_t)3 * nb * 2 * nzpml * c.nx * sizeof(T), st));
+    CK(cudaMemsetAsync(a.PX, 0, (size_t)nb * 2 * c.nz * nhx * sizeof(T), st));
+    CK(cudaMemsetAsync(a.SPX, 0, (size_t)3 * nb * 2 * c.nz * nhx * sizeof(T), st));
+    const int tm1 = time0 - 1;  // the first row pass of a step advances the counter
+    CK(cudaMemcpyAsync(p->d_time, &tm1, sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    return SPARC_OK;
+}
+
+bool check_cfg(const sparc_config_t *c, std::string &why)
+{
+    if (c->precision != 32 && c->precision != 64) { why = "precision must be 32 or 64"; return false; }
+    if (c->nbatch < 1) { why = "nbatch < 1"; return false; }
+    if (!fft_size_supported(c->nx)) { why = "nx not supported by the FFT (64..1024, 2^a 3^b)"; return false; }
+    const int cw = c->precision == 32 ? 32 : 16;
+    if (c->nx % cw) { why = "nx must be a multiple of the column width"; return false; }
+    if (c->nz < 16) { why = "nz < 16"; return false; }
+    if (c->npmlbot < 1 || c->npmltop < 1 || c->npmlbot + c->npmltop >= c->nz) { why = "bad vertical PML size"; return false; }
+    if (c->npmlhor < 1 || 2 * c->npmlhor >= c->nx) { why = "bad horizontal PML size"; return false; }
+    if (c->k_inj < 1 || c->k_inj > c->nz - 2 || c->k_obs < 0 || c->k_obs >= c->nz) { why = "bad injection/observation row"; return false; }
+    if (c->steps_out < 1) { why = "steps_out < 1"; return false; }
+    return true;
+}
+
+}  // namespace
+
+// ===============================================================================================
+// C ABI
+// ===============================================================================================
+extern "C" {
+
+const char *sparc_last_error(void) { return g_err.c_str(); }
+
+int sparc_plan_create(const sparc_config_t *cfg, sparc_plan_t **out)
+{
+    if (!cfg || !out) return fail(SPARC_ERR_ARG, "sparc_plan_create: null argument");
+    *out = nullptr;
+    std::string why;
+    if (!check_cfg(cfg, why)) return fail(SPARC_ERR_SIZE, "sparc_plan_create: " + why);
+    sparc_plan *p = new sparc_plan();
+    p->cfg = *cfg;
+    const int lmax = cfg->precision == 32 ? 32 : 16;
+    if (!chunking(cfg->nz, lmax, p->nch, p->L) || !chunking(cfg->nz, 16, p->nch64, p->L64)) {
+        delete p;
+        return fail(SPARC_ERR_SIZE, "sparc_plan_create: nz too large for the column chunking");
+    }
+    for (int ibc = 0; ibc < 4; ibc++) {
+        if (!build_ztab(cfg->nz, ibc, p->nch, p->L, p->hz[ibc]) ||
+            !build_ztab(cfg->nz, ibc, p->nch64, p->L64, p->hz64[ibc])) {
+            delete p;
+            return fail(SPARC_ERR_SIZE, "sparc_plan_create: singular reduced system");
+        }
+    }
+    cudaError_t e = cudaMalloc(&p->d_time, sizeof(int));
+    if (e != cudaSuccess) { delete p; return fail(SPARC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e)); }
+    p->allocs.push_back(p->d_time);
+    int zero = -1;
+    cudaMemcpy(p->d_time, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    for (int ibc = 0; ibc < 4; ibc++) {
+        e = upload_ztab<double>(p->hz64[ibc], p->z64[ibc], p->allocs);
+        if (e != cudaSuccess) { sparc_plan_destroy(p); return fail(SPARC_ERR_CUDA, std::string("tables: ") + cudaGetErrorString(e)); }
+    }
+    e = upload_fft<double>(cfg->nx, p->fft64, p->allocs);
+    if (e != cudaSuccess) { sparc_plan_destroy(p); return fail(SPARC_ERR_CUDA, std::string("fft: ") + cudaGetErrorString(e)); }
+    int rc = cfg->precision == 32 ? alloc_solver<float>(p) : alloc_solver<double>(p);
+    if (rc != SPARC_OK) { std::string m = g_err; sparc_plan_destroy(p); return fail(rc, m); }
+    *out = p;
+    return SPARC_OK;
+}
+
+int sparc_plan_destroy(sparc_plan_t *p)
+{
+    if (!p) return SPARC_OK;
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    free_solver(p->s32);
+    free_solver(p->s64);
+    for (void *q : p->allocs) cudaFree(q);
+    if (p->d_srcw) cudaFree(p->d_srcw);
+    if (p->d_srcidx) cudaFree(p->d_srcidx);
+    delete p;
+    return SPARC_OK;
+}
+
+int sparc_ddz(sparc_plan_t *p, const double *var, double *dvar, int n1, int ibc, const double *preset,
+              const double *stretch, void *stream)
+{
+    if (!p || !var || !dvar || n1 < 1) return fail(SPARC_ERR_ARG, "sparc_ddz: bad argument");
+    if (ibc < 0 || ibc > 3) return fail(SPARC_ERR_ARG, "sparc_ddz: ibc must be 0..3");
+    CK(launch_ddz<double>(p->z64[ibc].tab, p->nch64, p->L64, var, dvar, n1, p->cfg.nz, preset, stretch, 0,
+                          (cudaStream_t)stream));
+    return SPARC_OK;
+}
+
+int sparc_ddx(sparc_plan_t *p, const double *var, double *dvar, int nrows, double stretchx, void *stream)
+{
+    if (!p || !var || !dvar || nrows < 0) return fail(SPARC_ERR_ARG, "sparc_ddx: bad argument");
+    CK(launch_ddx<double>(var, dvar, nrows, p->cfg.nx, stretchx, p->fft64.twr, p->fft64.twi, p->fft64.kap,
+                          (cudaStream_t)stream));
+    return SPARC_OK;
+}
+
+int sparc_set_background(sparc_plan_t *p, const sparc_background_t *bg, void *stream)
+{
+    if (!p || !bg) return fail(SPARC_ERR_ARG, "sparc_set_background: null argument");
+    return p->cfg.precision == 32 ? set_background<float>(p, bg, (cudaStream_t)stream)
+                                  : set_background<double>(p, bg, (cudaStream_t)stream);
+}
+
+int sparc_set_source(sparc_plan_t *p, const double *inj_scale, const double *rows, int nrows, const double *wts,
+                     const int *idx, int ntab, void *stream)
+{
+    if (!p || !inj_scale || !rows || nrows < 1 || !wts || !idx || ntab < 1)
+        return fail(SPARC_ERR_ARG, "sparc_set_source: bad argument");
+    return p->cfg.precision == 32 ? set_source<float>(p, inj_scale, rows, nrows, wts, idx, ntab, (cudaStream_t)stream)
+                                  : set_source<double>(p, inj_scale, rows, nrows, wts, idx, ntab, (cudaStream_t)stream);
+}
+
+int sparc_reset_state(sparc_plan_t *p, int time0, void *stream)
+{
+    if (!p) return fail(SPARC_ERR_ARG, "sparc_reset_state: null plan");
+    return p->cfg.precision == 32 ? reset_state<float>(p, time0, (cudaStream_t)stream)
+                                  : reset_state<double>(p, time0, (cudaStream_t)stream);
+}
+
+int sparc_forward(sparc_plan_t *p, int nsteps, double flow_sign, void *seis, void *snaps, int nrec_cap,
+                  int use_graph, void *stream)
+{
+    if (!p || nsteps < 0 || nrec_cap < 0) return fail(SPARC_ERR_ARG, "sparc_forward: bad argument");
+    if (!p->have_bg || !p->have_src) return fail(SPARC_ERR_STATE, "sparc_forward: background and source must be set first");
+    if (nrec_cap > 0 && !seis && !snaps) return fail(SPARC_ERR_ARG, "sparc_forward: nrec_cap without outputs");
+    return p->cfg.precision == 32
+               ? run_forward<float>(p, nsteps, flow_sign, seis, snaps, nrec_cap, use_graph, (cudaStream_t)stream)
+               : run_forward<double>(p, nsteps, flow_sign, seis, snaps, nrec_cap, use_graph, (cudaStream_t)stream);
+}
+
+int sparc_get_state(sparc_plan_t *p, void *dst, void *stream)
+{
+    if (!p || !dst) return fail(SPARC_ERR_ARG, "sparc_get_state: bad argument");
+    const size_t es = p->cfg.precision == 32 ? 4 : 8;
+    const void *src = p->cfg.precision == 32 ? (const void *)p->s32.a.A : (const void *)p->s64.a.A;
+    CK(cudaMemcpyAsync(dst, src, (size_t)p->cfg.nbatch * 4 * p->cfg.nx * p->cfg.nz * es, cudaMemcpyDeviceToDevice,
+                       (cudaStream_t)stream));
+    return SPARC_OK;
+}
+
+int sparc_set_state(sparc_plan_t *p, const void *src, void *stream)
+{
+    if (!p || !src) return fail(SPARC_ERR_ARG, "sparc_set_state: bad argument");
+    const size_t es = p->cfg.precision == 32 ? 4 : 8;
+    void *dst = p->cfg.precision == 32 ? (void *)p->s32.a.A : (void *)p->s64.a.A;
+    CK(cudaMemcpyAsync(dst, src, (size_t)p->cfg.nbatch * 4 * p->cfg.nx * p->cfg.nz * es, cudaMemcpyDeviceToDevice,
+                       (cudaStream_t)stream));
+    return SPARC_OK;
+}
+
+int sparc_get_time(sparc_plan_t *p, int *time, void *stream)
+{
+    if (!p || !time) return fail(SPARC_ERR_ARG, "sparc_get_time: bad argument");
+    int t = 0;
+    CK(cudaMemcpyAsync(&t, p->d_time, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    *time = t + 1;
+    return SPARC_OK;
+}
+
+int sparc_kernels(sparc_plan_t *p, const void *fsn, int nfwd, const void *asn, int nadj, int npair, double *out,
+                  void *stream)
+{
+    (void)fsn; (void)nfwd; (void)asn; (void)nadj; (void)npair; (void)out; (void)stream;
+    if (!p) return fail(SPARC_ERR_ARG, "sparc_kernels: null plan");
+    return fail(SPARC_ERR_STATE, "sparc_kernels: not available in this build");
+}
+
+// Host evaluation of the partitioned compact-derivative tables (FP64), the same algebra the
+// device code applies; used to validate the tables without a GPU.
+int sparc_zsolve_host(int nz, int ibc, int lmax, const double *b, double *x, const double *preset, int n1)
+{
+    if (!b || !x || n1 < 1 || ibc < 0 || ibc > 3) return fail(SPARC_ERR_ARG, "sparc_zsolve_host: bad argument");
+    int nch, L;
+    if (!chunking(nz, lmax, nch, L)) return fail(SPARC_ERR_SIZE, "sparc_zsolve_host: bad chunking");
+    HostZTab t;
+    if (!build_ztab(nz, ibc, nch, L, t)) return fail(SPARC_ERR_SIZE, "sparc_zsolve_host: singular");
+    zsolve_host(t, b, x, preset, n1);
+    return SPARC_OK;
+}
+
+}  // extern "C"

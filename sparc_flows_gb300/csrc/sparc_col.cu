@@ -1,0 +1,411 @@
+// sparc_col.cu -- column (z-direction) passes of the RK step.
+//
+// A block owns CW adjacent x-columns of one solve over the full depth; its threads are CW
+// columns x NCH z-chunks.  Fields are staged in shared memory as [nz][CW] so every compact
+// derivative (dbyd2.f:8-235) reads its +-2 halo from shared memory, and the chunked Thomas
+// solves exchange only two boundary values per chunk (see sparc_common.cuh).
+//
+// col_stage_kernel, stage s (physics2d.f90:943-1094 in the order the data allow):
+//   xi_z(s) -> d/dz (ibc 3, top value -dxi_x/dx * unstretch) + vertical PML psi_vz
+//   div = dxi_x/dx + dxi_z/dz;  p = -c2rho0 div - gradp0_z xi_z;  rho = -rho0 div - gradrho0_z xi_z
+//   p -> d/dz (ibc 2) + vertical PML psi_p;  RHS v_z = -rhoinv (dp/dz + rho g) - 2 v0 . grad v_z + source
+//   v_x(s) -> d/dz (ibc 1): partial RHS v_x = -2 v0x dv_x/dx - 2 v0z dv_x/dz (completed by the next row pass)
+// end_step_kernel: a += deltat scr; FILTER_VARS_2D (physics2d.f90:509-556); pmlvars += deltat
+// scrpml; seismogram and partial-state records (driver.f90:386-417).
+#include "sparc_common.cuh"
+
+namespace sparc {
+
+// Column-block geometry: CW columns per block, at most MAXNCH chunks of at most LMAX rows.
+template <typename T>
+struct ColCfg;
+template <>
+struct ColCfg<float> {
+    static constexpr int CW = 32, LMAX = 32, MAXNCH = 12;
+};
+template <>
+struct ColCfg<double> {
+    static constexpr int CW = 16, LMAX = 16, MAXNCH = 20;
+};
+
+template <typename T>
+__device__ __forceinline__ T *svp(const StepArgs<T> &a, int slot, int b, int c)
+{
+    return a.SV + (((size_t)slot * a.nb + b) * 2 + c) * (size_t)a.nz * a.nx;
+}
+
+template <typename T>
+__device__ __forceinline__ int pml_row(const StepArgs<T> &a, int k)
+{
+    if (k < a.npmlbot) return k;
+    if (k >= a.nz - a.npmltop) return a.npmlbot + (k - (a.nz - a.npmltop));
+    return -1;
+}
+
+template <typename T, int CW, int LMAX>
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *B0 = reinterpret_cast<T *>(smem_raw);
+    const int nz = a.nz, nx = a.nx, nch = a.nch;
+    T *B1 = B0 + (size_t)nz * CW;
+    T *YB = B1 + (size_t)nz * CW;  // 4 x [2 nch][CW]
+    const int c = threadIdx.x % CW, j = threadIdx.x / CW;
+    const int x = blockIdx.x * CW + c;
+    const int b = blockIdx.y;
+    const int k0 = j * a.L;
+    const int n = min(a.L, nz - k0);
+    const size_t F = (size_t)nz * nx;
+    const T *Ab = a.A + (size_t)b * 4 * F;
+    const int s = a.stage;
+    const T bs = a.bs, bsm1 = a.bsm1;
+    const int time = *a.d_time;
+    T *yb0 = YB, *yb1 = YB + 2 * nch * CW, *yb2 = YB + 4 * nch * CW, *yb3 = YB + 6 * nch * CW;
+
+    T xz[LMAX];
+    // ---- A: xi_z at stage s (scr xi_z = v_z of stage s-1 with the RHS boundary zeros)
+#pragma unroll
+    for (int m = 0; m < LMAX; m++) {
+        if (m < n) {
+            const int k = k0 + m;
+            const size_t q = (size_t)k * nx + x;
+            T v = Ab[F_XIZ * F + q];
+            if (s >= 2) {
+                T avz = Ab[F_VZ * F + q];
+                T t = (s == 2) ? avz : avz + bsm1 * svp(a, a.slot_sm2, b, 1)[q];
+                if (k == 0 || x == 0 || x == nx - 1) t = T(0);
+                v += bs * t;
+            }
+            xz[m] = v;
+            B0[k * CW + c] = v;
+        }
+    }
+    __syncthreads();
+    // ---- B: local solve of d xi_z/dz
+    T y[LMAX];
+    const T preset3 = -a.TOPDX[(size_t)b * nx + x] * a.unstretch_top;
+    const T ylast_yb0 = zlocal<T, LMAX>(a.z3, B0, CW, c, k0, n, nz, preset3, y);
+    yb0[(2 * j) * CW + c] = y[0];
+    yb0[(2 * j + 1) * CW + c] = ylast_yb0;
+    __syncthreads();
+    // ---- C: correct, vertical PML, divergence, pressure
+    {
+        T xl, xr;
+        zcouple(a.z3, yb0, CW, c, j, nch, xl, xr);
+#pragma unroll
+        for (int m = 0; m < LMAX; m++) {
+            if (m < n) {
+                const int k = k0 + m;
+                const size_t q = (size_t)k * nx + x;
+                T dzz = zcorrect(a.z3, y[m], k, xl, xr) * __ldg(a.stretch + k);
+                const int pi = pml_row(a, k);
+                T fd = T(1);
+                if (pi >= 0) {
+                    const size_t qz = ((size_t)b * 2 * a.nzpml + pi) * nx + x;  // psi_vz
+                    const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
+                    T ps = a.PZ[qz];
+                    if (s >= 2) ps += bs * a.SPZ[(size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz];
+                    a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz] = __ldg(a.az + qb) * dzz + __ldg(a.bz + qb) * ps;
+                    dzz += ps;
+                    fd = __ldg(a.fdz + qb);
+                }
+                const T div = a.DX[(size_t)b * F + q] + dzz;
+                const T c2r = a.c2d ? __ldg(a.c2rho0 + (size_t)b * a.bg2 + q) : __ldg(a.c2rho0 + k);
+                const T gp = __ldg(a.gp0 + k) * fd, gr = __ldg(a.gr0 + k) * fd;
+                const T p = -c2r * div - gp * xz[m];
+                const T rho = -__ldg(a.rho0 + k) * div - gr * xz[m];
+                xz[m] = rho * __ldg(a.g + k);
+                B1[k * CW + c] = p;
+                a.P[(size_t)b * F + q] = p;
+                T vx = Ab[F_VX * F + q];
+                if (s >= 2) vx += bs * svp(a, a.slot_sm1, b, 0)[q];
+                B0[k * CW + c] = vx;
+            }
+        }
+    }
+    __syncthreads();
+    // ---- D: local solves of dp/dz (ibc 2, bottom value 0) and dv_x/dz (ibc 1)
+    T y2[LMAX];
+    const T ylast_yb1 = zlocal<T, LMAX>(a.z2, B1, CW, c, k0, n, nz, T(0), y);
+    yb1[(2 * j) * CW + c] = y[0];
+    yb1[(2 * j + 1) * CW + c] = ylast_yb1;
+    if (a.flows) {
+        const T y2last_yb2 = zlocal<T, LMAX>(a.z1, B0, CW, c, k0, n, nz, T(0), y2);
+        yb2[(2 * j) * CW + c] = y2[0];
+        yb2[(2 * j + 1) * CW + c] = y2last_yb2;
+    }
+    __syncthreads();
+    // ---- E: gradient of p, RHS v_z without advection; advection of v_x along z
+    {
+        T xl, xr;
+        zcouple(a.z2, yb1, CW, c, j, nch, xl, xr);
+        T xl2 = T(0), xr2 = T(0);
+        if (a.flows) zcouple(a.z1, yb2, CW, c, j, nch, xl2, xr2);
+#pragma unroll
+        for (int m = 0; m < LMAX; m++) {
+            if (m < n) {
+                const int k = k0 + m;
+                const size_t q = (size_t)k * nx + x;
+                T gpz = zcorrect(a.z2, y[m], k, xl, xr) * __ldg(a.stretch + k);
+                const int pi = pml_row(a, k);
+                if (pi >= 0) {
+                    const size_t qz = (((size_t)b * 2 + 1) * a.nzpml + pi) * nx + x;  // psi_p
+                    const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
+                    T ps = a.PZ[qz];
+                    if (s >= 2) ps += bs * a.SPZ[(size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz];
+                    a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz] = __ldg(a.az + qb) * gpz + __ldg(a.bz + qb) * ps;
+                    gpz += ps;
+                }
+                xz[m] = -__ldg(a.rhoinv + k) * (gpz + xz[m]);
+                T rv = T(0);
+                if (a.flows) {
+                    const T dvxdz = zcorrect(a.z1, y2[m], k, xl2, xr2) * __ldg(a.stretch + k);
+                    rv = a.FXX[(size_t)b * F + q] - T(2) * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvxdz;
+                }
+                a.RVXP[(size_t)b * F + q] = rv;
+                T vz = Ab[F_VZ * F + q];
+                if (s >= 2) vz += bs * svp(a, a.slot_sm1, b, 1)[q];
+                B1[k * CW + c] = vz;
+            }
+        }
+    }
+    __syncthreads();
+    // ---- F: local solve of dv_z/dz
+    if (a.flows) {
+        const T y2last_yb3 = zlocal<T, LMAX>(a.z1, B1, CW, c, k0, n, nz, T(0), y2);
+        yb3[(2 * j) * CW + c] = y2[0];
+        yb3[(2 * j + 1) * CW + c] = y2last_yb3;
+    }
+    __syncthreads();
+    // ---- G: finish RHS v_z (advection, source, boundary zeros)
+    T xl2 = T(0), xr2 = T(0);
+    if (a.flows) zcouple(a.z1, yb3, CW, c, j, nch, xl2, xr2);
+    T forcing = T(0);
+    const bool inject = (time <= a.src_until) && (time >= 0) && (time < a.ntab);
+    if (inject && a.k_inj >= k0 && a.k_inj < k0 + n) {
+        const double *w = a.src_w + (size_t)time * 7;
+        const int i0 = a.src_idx[time];
+        double f = 0.0;
+        for (int jj = 0; jj < 7; jj++) {
+            const int r = i0 + jj;
+            if (r >= 0 && r < a.nrows && w[jj] != 0.0)
+                f += w[jj] * (double)a.src_rows[((size_t)b * a.nrows + r) * nx + x];
+        }
+        forcing = T(f) * a.inj_scale[(size_t)b * nx + x];
+    }
+    T *svz = svp(a, a.slot_s, b, 1);
+#pragma unroll
+    for (int m = 0; m < LMAX; m++) {
+        if (m < n) {
+            const int k = k0 + m;
+            const size_t q = (size_t)k * nx + x;
+            T r = xz[m];
+            if (k == a.k_inj) r += forcing;
+            if (a.flows) {
+                const T dvzdz = zcorrect(a.z1, y2[m], k, xl2, xr2) * __ldg(a.stretch + k);
+                r += a.FXZ[(size_t)b * F + q] - T(2) * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvzdz;
+            }
+            if (k == 0 || x == 0 || x == nx - 1) r = T(0);
+            svz[q] = r;
+        }
+    }
+}
+
+// FILTER_VARS_2D coefficients (physics2d.f90:517-522), already halved for the neighbours.
+template <typename T>
+__device__ __forceinline__ T filt11(const T *B, int CW, int c, int k)
+{
+    const T c0 = T(0.75390625), h1 = T(0.5 * 0.41015625), h2 = T(0.5 * -0.234375), h3 = T(0.5 * 0.087890625),
+            h4 = T(0.5 * -0.01953125), h5 = T(0.5 * 0.001953125);
+    return c0 * B[k * CW + c] + h1 * (B[(k - 1) * CW + c] + B[(k + 1) * CW + c]) +
+           h2 * (B[(k - 2) * CW + c] + B[(k + 2) * CW + c]) + h3 * (B[(k - 3) * CW + c] + B[(k + 3) * CW + c]) +
+           h4 * (B[(k - 4) * CW + c] + B[(k + 4) * CW + c]) + h5 * (B[(k - 5) * CW + c] + B[(k + 5) * CW + c]);
+}
+
+template <typename T, int CW, int LMAX>
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) end_step_kernel(StepArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *B0 = reinterpret_cast<T *>(smem_raw);
+    const int nz = a.nz, nx = a.nx;
+    const int c = threadIdx.x % CW, j = threadIdx.x / CW;
+    const int x = blockIdx.x * CW + c;
+    const int b = blockIdx.y;
+    const int k0 = j * a.L;
+    const int n = min(a.L, nz - k0);
+    const size_t F = (size_t)nz * nx;
+    T *Ab = a.A + (size_t)b * 4 * F;
+    const int time = *a.d_time;
+    const int rec = (a.steps_out > 0) ? time / a.steps_out : 0;
+    const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec < a.nrec_cap && time >= 0;
+    const bool xf = (x >= a.nh - 1) && (x <= nx - a.nh);
+    T *snap = record && a.snaps ? a.snaps + ((size_t)b * a.nrec_cap + rec) * 6 * F : nullptr;
+    for (int f = 0; f < 4; f++) {
+        for (int m = 0; m < n; m++) {
+            {
+                const int k = k0 + m;
+                const size_t q = (size_t)k * nx + x;
+                T sc;
+                if (f == F_XIX || f == F_XIZ) {  // scr xi = v of stage 5 with the RHS boundary zeros
+                    const int cc = (f == F_XIX) ? 0 : 1;
+                    sc = Ab[(f == F_XIX ? F_VX : F_VZ) * F + q] + a.bs * svp(a, a.slot_sm1, b, cc)[q];
+                    if (k == 0 || x == 0 || x == nx - 1) sc = T(0);
+                } else {
+                    sc = svp(a, a.slot_s, b, f == F_VX ? 0 : 1)[q];
+                }
+                B0[k * CW + c] = Ab[f * F + q] + a.dt * sc;
+            }
+        }
+        __syncthreads();
+        for (int m = 0; m < n; m++) {
+            {
+                const int k = k0 + m;
+                const size_t q = (size_t)k * nx + x;
+                T out = B0[k * CW + c];
+                if (xf && k >= 5 && k <= nz - 2) {
+                    if (k <= nz - 6) out = filt11(B0, CW, c, k);
+                    else out = T(0.5) * (B0[(k + 1) * CW + c] + B0[(k - 1) * CW + c]);
+                }
+                Ab[f * F + q] = out;
+                if (snap) snap[(size_t)f * F + q] = out;
+                if (record && f == F_VZ && k == a.k_obs && a.seis)
+                    a.seis[((size_t)b * a.nrec_cap + rec) * nx + x] = out;
+            }
+        }
+        __syncthreads();
+    }
+    for (int m = 0; m < n; m++) {
+        {
+            const int k = k0 + m;
+            const size_t q = (size_t)k * nx + x;
+            const int pi = pml_row(a, k);
+            if (pi >= 0) {
+                for (int cc = 0; cc < 2; cc++) {
+                    const size_t qz = (((size_t)b * 2 + cc) * a.nzpml + pi) * nx + x;
+                    a.PZ[qz] += a.dt * a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz];
+                }
+            }
+            if (snap) {
+                snap[4 * F + q] = svp(a, a.slot_s, b, 0)[q];
+                snap[5 * F + q] = svp(a, a.slot_s, b, 1)[q];
+            }
+        }
+    }
+}
+
+// Generic compact derivative of n1 columns: dvar = stretch .* dbyd2(var), optional
+// FILTER_VAR_Z (kernels.f90:891-928) afterwards.
+template <typename T, int CW, int LMAX>
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) ddz_kernel(ZTab<T> tb, int nch, int L, const T *__restrict__ var,
+                                                         T *__restrict__ dvar, int n1, int nz,
+                                                         const T *__restrict__ preset,
+                                                         const T *__restrict__ stretch, int filter)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *B0 = reinterpret_cast<T *>(smem_raw);
+    T *YB = B0 + (size_t)nz * CW;
+    const int c = threadIdx.x % CW, j = threadIdx.x / CW;
+    const int x = blockIdx.x * CW + c;
+    const bool valid = x < n1;
+    const int xs = valid ? x : n1 - 1;
+    const int k0 = j * L;
+    const int n = min(L, nz - k0);
+#pragma unroll
+    for (int m = 0; m < LMAX; m++)
+        if (m < n) B0[(k0 + m) * CW + c] = var[(size_t)(k0 + m) * n1 + xs];
+    __syncthreads();
+    T y[LMAX];
+    const T pre = preset ? preset[xs] : T(0);
+    const T ylast_YB = zlocal<T, LMAX>(tb, B0, CW, c, k0, n, nz, pre, y);
+    YB[(2 * j) * CW + c] = y[0];
+    YB[(2 * j + 1) * CW + c] = ylast_YB;
+    __syncthreads();
+    T xl, xr;
+    zcouple(tb, YB, CW, c, j, nch, xl, xr);
+#pragma unroll
+    for (int m = 0; m < LMAX; m++) {
+        if (m < n) {
+            const int k = k0 + m;
+            y[m] = zcorrect(tb, y[m], k, xl, xr) * (stretch ? __ldg(stretch + k) : T(1));
+        }
+    }
+    if (filter) {
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < LMAX; m++)
+            if (m < n) B0[(k0 + m) * CW + c] = y[m];
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < LMAX; m++) {
+            if (m < n) {
+                const int k = k0 + m;
+                if (k >= 1 && k <= 4) y[m] = T(0.5) * (B0[(k + 1) * CW + c] + B0[(k - 1) * CW + c]);
+                else if (k >= 5 && k <= nz - 6) y[m] = filt11(B0, CW, c, k);
+                else if (k >= nz - 5 && k <= nz - 2) y[m] = T(0.5) * (B0[(k + 1) * CW + c] + B0[(k - 1) * CW + c]);
+            }
+        }
+    }
+    if (valid) {
+#pragma unroll
+        for (int m = 0; m < LMAX; m++)
+            if (m < n) dvar[(size_t)(k0 + m) * n1 + x] = y[m];
+    }
+}
+
+
+template <typename T>
+static size_t col_smem(int nz, int nch)
+{
+    return ((size_t)2 * nz * ColCfg<T>::CW + (size_t)8 * nch * ColCfg<T>::CW) * sizeof(T);
+}
+
+template <typename T>
+cudaError_t launch_col_stage(const StepArgs<T> &a, cudaStream_t st)
+{
+    constexpr int CW = ColCfg<T>::CW, LMAX = ColCfg<T>::LMAX;
+    if (a.nx % CW || a.L > LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
+    const size_t smem = col_smem<T>(a.nz, a.nch);
+    auto k = col_stage_kernel<T, CW, LMAX>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid(a.nx / CW, a.nb);
+    k<<<grid, CW * a.nch, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_end_step(const StepArgs<T> &a, cudaStream_t st)
+{
+    constexpr int CW = ColCfg<T>::CW, LMAX = ColCfg<T>::LMAX;
+    if (a.nx % CW || a.L > LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)a.nz * CW * sizeof(T);
+    auto k = end_step_kernel<T, CW, LMAX>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid(a.nx / CW, a.nb);
+    k<<<grid, CW * a.nch, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_ddz(const ZTab<T> &tb, int nch, int L, const T *var, T *dvar, int n1, int nz, const T *preset,
+                       const T *stretch, int filter, cudaStream_t st)
+{
+    constexpr int CW = ColCfg<T>::CW, LMAX = ColCfg<T>::LMAX;
+    if (L > LMAX || nch > ColCfg<T>::MAXNCH || n1 <= 0) return cudaErrorInvalidValue;
+    const size_t smem = ((size_t)nz * CW + (size_t)2 * nch * CW) * sizeof(T);
+    auto k = ddz_kernel<T, CW, LMAX>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((n1 + CW - 1) / CW);
+    k<<<grid, CW * nch, smem, st>>>(tb, nch, L, var, dvar, n1, nz, preset, stretch, filter);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_col_stage<float>(const StepArgs<float> &, cudaStream_t);
+template cudaError_t launch_col_stage<double>(const StepArgs<double> &, cudaStream_t);
+template cudaError_t launch_end_step<float>(const StepArgs<float> &, cudaStream_t);
+template cudaError_t launch_end_step<double>(const StepArgs<double> &, cudaStream_t);
+template cudaError_t launch_ddz<float>(const ZTab<float> &, int, int, const float *, float *, int, int,
+                                       const float *, const float *, int, cudaStream_t);
+template cudaError_t launch_ddz<double>(const ZTab<double> &, int, int, const double *, double *, int, int,
+                                        const double *, const double *, int, cudaStream_t);
+
+}  // namespace sparc

@@ -1,0 +1,281 @@
+// sparc_common.cuh -- device data structures and building blocks of the GB300 wave solver.
+//
+//  * warp-level Stockham FFT (radix 4/2/3, shared-memory ping-pong) used for the spectral
+//    x-derivative of derivatives.f90:28-58;
+//  * SPIKE-partitioned solve of the sixth-order compact z-derivative (dbyd2.f:8-235,
+//    mtridag.f:96-112): each column is cut into NCH chunks of at most LMAX rows, every chunk
+//    is solved independently with its own Thomas factors, and the coupling between chunks is
+//    restored exactly through precomputed spike vectors and the inverse of the small reduced
+//    system (all factors precomputed in FP64 on the host).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace sparc {
+
+constexpr int WARP = 32;
+constexpr int MAX_NCH = 24;  // chunks per column (nz <= MAX_NCH * LMAX)
+
+// Field order of the live state (xi_y and v_y vanish identically in 2-D).
+enum { F_XIX = 0, F_XIZ = 1, F_VX = 2, F_VZ = 3 };
+
+// Compact-derivative tables for one boundary condition (device pointers).
+template <typename T>
+struct ZTab {
+    const T *w5;    // [nz][5] stencil weights of rows 0, 1, nz-2, nz-1 (rows 0,1 on b[0..4],
+                    // rows nz-2, nz-1 on b[nz-5..nz-1]); interior rows use c1, c2
+    const T *ib;    // [nz] 1/beta of the chunk-local Thomas factorisation
+    const T *lwib;  // [nz] lower * ib
+    const T *gm;    // [nz] gamma (backward sweep)
+    const T *WL;    // [nz] lower(s_c) * spike from the chunk's first row
+    const T *VU;    // [nz] upper(e_c) * spike from the chunk's last row
+    const T *G;     // [2 nch][2 nch] inverse of the reduced system
+    T c1, c2;       // interior coefficients (float32 values of dbyd2.f:82-83)
+    int preset_row; // row whose right-hand side is supplied by the caller (-1: none)
+};
+
+// Everything one stage kernel needs.  Layouts (x fastest everywhere):
+//   A    [nb][4][nz][nx]            state xi_x, xi_z, v_x, v_z
+//   SV   [3][nb][2][nz][nx]         ring of stage RHS of v_x, v_z (slot = stage % 3)
+//   P, RVXP, DX, FXX, FXZ [nb][nz][nx] stage intermediates, TOPDX [nb][nx]
+//   PZ   [nb][2][nzpml][nx]         psi_vz, psi_p;  SPZ [3][nb][2][nzpml][nx]
+//   PX   [nb][2][nz][nhx]           psi_vx, psi_gradp_x;  SPX [3][nb][2][nz][nhx]
+template <typename T>
+struct StepArgs {
+    int nx, nz, nb, nh, nhx, nzpml, npmlbot, npmltop;
+    int flows, c2d;
+    long long bg2, bgz, bgx;  // batch strides of 2-D, PML-layer and x-PML background arrays
+    T bs, bsm1, dt, stretchx, fsign, unstretch_top;
+    int stage, slot_s, slot_sm1, slot_sm2;
+    T *A, *SV, *P, *RVXP, *DX, *FXX, *FXZ, *TOPDX, *PZ, *SPZ, *PX, *SPX;
+    const T *rhoinv, *rho0, *gp0, *gr0, *g, *stretch;
+    const T *fdz, *az, *bz, *ax, *bx, *c2rho0, *v0x, *v0z;
+    const T *twr, *twi, *kap;
+    ZTab<T> z1, z2, z3;
+    int nch, L;
+    int *d_time;
+    int src_until, k_inj, k_obs, steps_out;
+    const T *inj_scale, *src_rows;
+    int nrows;
+    const double *src_w;
+    const int *src_idx;
+    int ntab;
+    T *seis, *snaps;
+    int nrec_cap;
+};
+
+// ------------------------------------------------------------------------------------------
+// FFT
+// ------------------------------------------------------------------------------------------
+template <int N>
+struct Radices {
+    static constexpr int count()
+    {
+        int n = N, c = 0;
+        while (n % 4 == 0) { n /= 4; c++; }
+        while (n % 2 == 0) { n /= 2; c++; }
+        while (n % 3 == 0) { n /= 3; c++; }
+        return c;
+    }
+    static constexpr int at(int i)
+    {
+        int n = N, c = 0;
+        while (n % 4 == 0) { if (c == i) return 4; n /= 4; c++; }
+        while (n % 2 == 0) { if (c == i) return 2; n /= 2; c++; }
+        while (n % 3 == 0) { if (c == i) return 3; n /= 3; c++; }
+        return 1;
+    }
+};
+
+template <typename T, int R>
+__device__ __forceinline__ void butterfly(T *vr, T *vi, bool inv)
+{
+    if constexpr (R == 2) {
+        T ar = vr[0], ai = vi[0];
+        vr[0] = ar + vr[1]; vi[0] = ai + vi[1];
+        vr[1] = ar - vr[1]; vi[1] = ai - vi[1];
+    } else if constexpr (R == 4) {
+        T s0r = vr[0] + vr[2], s0i = vi[0] + vi[2];
+        T d0r = vr[0] - vr[2], d0i = vi[0] - vi[2];
+        T s1r = vr[1] + vr[3], s1i = vi[1] + vi[3];
+        T d1r = vr[1] - vr[3], d1i = vi[1] - vi[3];
+        T jr = inv ? -d1i : d1i, ji = inv ? d1r : -d1r;  // d1 * (inv ? +i : -i)
+        vr[0] = s0r + s1r; vi[0] = s0i + s1i;
+        vr[1] = d0r + jr;  vi[1] = d0i + ji;
+        vr[2] = s0r - s1r; vi[2] = s0i - s1i;
+        vr[3] = d0r - jr;  vi[3] = d0i - ji;
+    } else {  // R == 3
+        const T h = T(0.8660254037844386467637231707529362);
+        T tr = vr[1] + vr[2], ti = vi[1] + vi[2];
+        T dr = vr[1] - vr[2], di = vi[1] - vi[2];
+        T mr = vr[0] - T(0.5) * tr, mi = vi[0] - T(0.5) * ti;
+        T sg = inv ? h : -h;  // sigma * sqrt(3)/2
+        // i * sg * d = (-sg*di, sg*dr)
+        vr[0] = vr[0] + tr; vi[0] = vi[0] + ti;
+        vr[1] = mr - sg * di; vi[1] = mi + sg * dr;
+        vr[2] = mr + sg * di; vi[2] = mi - sg * dr;
+    }
+}
+
+// One Stockham autosort stage of radix R after NS points have been combined.
+template <typename T, int N, int R, int NS>
+__device__ __forceinline__ void stockham_stage(const T *__restrict__ xr, const T *__restrict__ xi,
+                                               T *__restrict__ yr, T *__restrict__ yi,
+                                               const T *__restrict__ twr, const T *__restrict__ twi,
+                                               int lane, bool inv)
+{
+    constexpr int NR = N / R;
+    constexpr int TS = N / (NS * R);
+#pragma unroll 2
+    for (int j = lane; j < NR; j += WARP) {
+        const int k = j % NS;
+        T vr[R], vi[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            T ar = xr[j + r * NR], ai = xi[j + r * NR];
+            if (NS == 1 || r == 0) {
+                vr[r] = ar; vi[r] = ai;
+            } else {
+                const int t = r * k * TS;  // < N
+                T wr = __ldg(twr + t), wi = __ldg(twi + t);
+                if (inv) wi = -wi;
+                vr[r] = ar * wr - ai * wi;
+                vi[r] = ar * wi + ai * wr;
+            }
+        }
+        butterfly<T, R>(vr, vi, inv);
+        const int base = (j / NS) * NS * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            yr[base + r * NS] = vr[r];
+            yi[base + r * NS] = vi[r];
+        }
+    }
+}
+
+template <typename T, int N, int I, int NS>
+struct FFTRun {
+    __device__ static __forceinline__ void run(T *xr, T *xi, T *yr, T *yi, const T *twr, const T *twi,
+                                               int lane, bool inv, T *&outr, T *&outi)
+    {
+        if constexpr (I == Radices<N>::count()) {
+            outr = xr; outi = xi;
+        } else {
+            constexpr int R = Radices<N>::at(I);
+            stockham_stage<T, N, R, NS>(xr, xi, yr, yi, twr, twi, lane, inv);
+            __syncwarp();
+            FFTRun<T, N, I + 1, NS * R>::run(yr, yi, xr, xi, twr, twi, lane, inv, outr, outi);
+        }
+    }
+};
+
+// Spectral derivative of the complex row (xr + i xi) of length N held in warp-private shared
+// memory (yr, yi are scratch of the same size): forward FFT, multiply bin k by
+// i*kap[k]*scale (kap already carries the 1/N normalisation and a zero Nyquist bin), inverse
+// FFT.  Real and imaginary parts of the result are the derivatives of the two real rows.
+template <typename T, int N>
+__device__ __forceinline__ void fft_deriv(T *xr, T *xi, T *yr, T *yi, const T *twr, const T *twi,
+                                          const T *kap, T scale, int lane, T *&outr, T *&outi)
+{
+    T *fr, *fi;
+    FFTRun<T, N, 0, 1>::run(xr, xi, yr, yi, twr, twi, lane, false, fr, fi);
+    for (int k = lane; k < N; k += WARP) {
+        T kk = __ldg(kap + k) * scale;
+        T re = fr[k], im = fi[k];
+        fr[k] = -kk * im;
+        fi[k] = kk * re;
+    }
+    __syncwarp();
+    T *gr = (fr == xr) ? yr : xr, *gi = (fr == xr) ? yi : xi;
+    FFTRun<T, N, 0, 1>::run(fr, fi, gr, gi, twr, twi, lane, true, outr, outi);
+}
+
+// ------------------------------------------------------------------------------------------
+// Compact z-derivative, SPIKE-partitioned (see file comment).
+// src: shared memory [nz][CWS] (column stride CWS), thread owns rows [k0, k0+n) of column c.
+// ------------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T zrhs(const ZTab<T> &tb, const T *src, int CWS, int c, int k, int nz, T preset)
+{
+    if (k >= 2 && k <= nz - 3)
+        return tb.c1 * (src[(k + 1) * CWS + c] - src[(k - 1) * CWS + c]) +
+               tb.c2 * (src[(k + 2) * CWS + c] - src[(k - 2) * CWS + c]);
+    if (k == tb.preset_row) return preset;
+    const int base = (k <= 1) ? 0 : nz - 5;
+    const T *w = tb.w5 + 5 * k;
+    T r = __ldg(w) * src[base * CWS + c];
+#pragma unroll
+    for (int j = 1; j < 5; j++) r += __ldg(w + j) * src[(base + j) * CWS + c];
+    return r;
+}
+
+// Chunk-local forward and backward sweeps; y[m] for m < n.  Returns y[n-1] (kept out of
+// the register array so that it is never indexed with a run-time value).
+template <typename T, int LMAX>
+__device__ __forceinline__ T zlocal(const ZTab<T> &tb, const T *src, int CWS, int c, int k0, int n, int nz,
+                                    T preset, T (&y)[LMAX])
+{
+    T prev = T(0);
+#pragma unroll
+    for (int m = 0; m < LMAX; m++) {
+        if (m < n) {
+            const int k = k0 + m;
+            T v = zrhs(tb, src, CWS, c, k, nz, preset) * __ldg(tb.ib + k);
+            if (m > 0) v -= __ldg(tb.lwib + k) * prev;
+            y[m] = v;
+            prev = v;
+        }
+    }
+    const T last = prev;
+#pragma unroll
+    for (int m = LMAX - 2; m >= 0; m--) {
+        if (m + 1 < n) y[m] -= __ldg(tb.gm + k0 + m + 1) * y[m + 1];
+    }
+    return last;
+}
+
+// Coupling values from the neighbouring chunks: xl = x[first row - 1], xr = x[last row + 1].
+template <typename T>
+__device__ __forceinline__ void zcouple(const ZTab<T> &tb, const T *ybnd, int CWS, int c, int j, int nch,
+                                        T &xl, T &xr)
+{
+    const int n2 = 2 * nch;
+    xl = T(0); xr = T(0);
+    if (j > 0) {
+        const T *g = tb.G + (2 * j - 1) * n2;
+        for (int q = 0; q < n2; q++) xl += __ldg(g + q) * ybnd[q * CWS + c];
+    }
+    if (j < nch - 1) {
+        const T *g = tb.G + (2 * j + 2) * n2;
+        for (int q = 0; q < n2; q++) xr += __ldg(g + q) * ybnd[q * CWS + c];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T zcorrect(const ZTab<T> &tb, T y, int k, T xl, T xr)
+{
+    return y - __ldg(tb.WL + k) * xl - __ldg(tb.VU + k) * xr;
+}
+
+// ------------------------------------------------------------------------------------------
+// Launchers (defined in sparc_row.cu / sparc_col.cu)
+// ------------------------------------------------------------------------------------------
+template <typename T>
+cudaError_t launch_row_stage(const StepArgs<T> &a, cudaStream_t st);
+template <typename T>
+cudaError_t launch_col_stage(const StepArgs<T> &a, cudaStream_t st);
+template <typename T>
+cudaError_t launch_end_step(const StepArgs<T> &a, cudaStream_t st);
+template <typename T>
+cudaError_t launch_ddx(const T *var, T *dvar, int nrows, int nx, T stretchx, const T *twr, const T *twi,
+                       const T *kap, cudaStream_t st);
+template <typename T>
+cudaError_t launch_ddz(const ZTab<T> &tb, int nch, int L, const T *var, T *dvar, int n1, int nz,
+                       const T *preset, const T *stretch, int filter, cudaStream_t st);
+template <typename T>
+cudaError_t launch_kernel_accum(const StepArgs<T> &a, const T *fsn, int nfwd, const T *asn, int nadj, int npair,
+                                double *out, T *work, cudaStream_t st);
+
+bool fft_size_supported(int n);
+
+}  // namespace sparc

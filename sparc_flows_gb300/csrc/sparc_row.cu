@@ -1,0 +1,223 @@
+// sparc_row.cu -- row (x-direction) passes of the RK stage: spectral x-derivatives
+// (derivatives.f90:28-58) with the horizontal PML (physics2d.f90:970-986, 1003-1020).
+//
+// One warp owns one x-row of one solve.  Two real rows are differentiated by one complex
+// FFT (real part + i * imaginary part), the derivative operator mapping real rows to real
+// rows.  Stage s of the RK step needs, along x:
+//   d/dx of p from stage s-1   -> completes RHS v_x of stage s-1 (-rhoinv * dp/dx);
+//   d/dx of xi_x at stage s    -> divergence input of stage s (plus the top-row value that
+//                                 the column pass needs for its ibc=3 boundary);
+//   d/dx of v_x, v_z at stage s -> advection terms -2 v0x d/dx (physics2d.f90:1065-1079).
+#include "sparc_common.cuh"
+
+namespace sparc {
+
+constexpr int ROW_WPB = 4;  // rows (warps) per block
+
+template <typename T>
+__device__ __forceinline__ T *svp(const StepArgs<T> &a, int slot, int b, int c)
+{
+    return a.SV + (((size_t)slot * a.nb + b) * 2 + c) * (size_t)a.nz * a.nx;
+}
+
+// MODE 0: stage 1 (no pressure yet), MODE 1: stages 2..5, MODE 2: closing pass after stage 5.
+template <typename T, int N, int MODE>
+__global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (MODE == 0 && blockIdx.x == 0 && threadIdx.x == 0) *a.d_time += 1;  // new step begins
+    const int row = blockIdx.x * ROW_WPB + warp;
+    if (row >= a.nb * a.nz) return;
+    T *xr = sm + warp * 4 * N, *xi = xr + N, *yr = xi + N, *yi = yr + N;
+    const int b = row / a.nz, k = row - b * a.nz;
+    const int nx = N, nh = a.nh, nhx = a.nhx;
+    const size_t F = (size_t)a.nz * nx;
+    const size_t ro = (size_t)k * nx;
+    const T *Ab = a.A + (size_t)b * 4 * F;
+    const T bs = a.bs, bsm1 = a.bsm1;
+    const T rhoinv_k = __ldg(a.rhoinv + k);
+    T *PXb = a.PX + (size_t)b * 2 * a.nz * nhx;
+    const T *axk = a.ax + (size_t)b * a.bgx + (size_t)k * nhx;
+    const T *bxk = a.bx + (size_t)b * a.bgx + (size_t)k * nhx;
+
+    // ---- load: (p_{s-1}, xi_x at stage s) or (p_5, 0)
+    for (int x = lane; x < nx; x += WARP) {
+        T p = T(0), xis = T(0);
+        if (MODE != 0) p = a.P[(size_t)b * F + ro + x];
+        if (MODE == 0) {
+            xis = Ab[F_XIX * F + ro + x];
+        } else if (MODE == 1) {
+            T avx = Ab[F_VX * F + ro + x];
+            T s = (a.stage == 2) ? avx : avx + bsm1 * svp(a, a.slot_sm2, b, 0)[ro + x];
+            if (k == 0 || x == 0 || x == nx - 1) s = T(0);  // RHS boundary zeros (physics2d.f90:1083-1093)
+            xis = Ab[F_XIX * F + ro + x] + bs * s;
+        }
+        xr[x] = p;
+        xi[x] = xis;
+    }
+    __syncwarp();
+    T *o1r, *o1i;
+    fft_deriv<T, N>(xr, xi, yr, yi, a.twr, a.twi, a.kap, a.stretchx, lane, o1r, o1i);
+    __syncwarp();
+
+    for (int x = lane; x < nx; x += WARP) {
+        T gpx = o1r[x], dxx = o1i[x];
+        const bool pml = (x < nh) || (x >= nx - nh);
+        const int ai = (x < nh) ? x : x - (nx - nh) + nh;
+        if (MODE != 2 && k == a.nz - 1) a.TOPDX[(size_t)b * nx + x] = dxx;
+        if (pml) {
+            const T axv = __ldg(axk + ai), bxv = __ldg(bxk + ai);
+            if (MODE != 0) {  // psi_gradp_x of stage s-1
+                const size_t q = ((size_t)1 * a.nz + k) * nhx + ai;
+                T ps = PXb[q];
+                if (a.stage >= 3) ps += bsm1 * a.SPX[((size_t)a.slot_sm2 * a.nb + b) * 2 * a.nz * nhx + q];
+                gpx += ps;
+                a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q] = axv * gpx + bxv * ps;
+            }
+            if (MODE != 2) {  // psi_vx of stage s
+                const size_t q = ((size_t)0 * a.nz + k) * nhx + ai;
+                T ps = PXb[q];
+                if (MODE == 1) ps += bs * a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q];
+                dxx += ps;
+                a.SPX[((size_t)a.slot_s * a.nb + b) * 2 * a.nz * nhx + q] = axv * dxx + bxv * ps;
+            }
+        }
+        T svx = T(0);
+        if (MODE != 0) {
+            svx = a.RVXP[(size_t)b * F + ro + x] - rhoinv_k * gpx;
+            if (k == 0 || x == 0 || x == nx - 1) svx = T(0);
+            svp(a, a.slot_sm1, b, 0)[ro + x] = svx;
+        }
+        if (MODE != 2) {
+            a.DX[(size_t)b * F + ro + x] = dxx;
+            T vxs = Ab[F_VX * F + ro + x], vzs = Ab[F_VZ * F + ro + x];
+            if (MODE == 1) {
+                vxs += bs * svx;
+                vzs += bs * svp(a, a.slot_sm1, b, 1)[ro + x];
+            }
+            o1r[x] = vxs;
+            o1i[x] = vzs;
+        } else if (pml) {
+            // closing pass: pmlvarsx += deltat * scrpmlx (step.f90:112-115)
+            for (int c = 0; c < 2; c++) {
+                const size_t q = ((size_t)c * a.nz + k) * nhx + ai;
+                PXb[q] += a.dt * a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q];
+            }
+        }
+    }
+    if (MODE == 2 || !a.flows) return;
+    __syncwarp();
+    T *gr = (o1r == xr) ? yr : xr, *gi = (o1r == xr) ? yi : xi;
+    T *o2r, *o2i;
+    fft_deriv<T, N>(o1r, o1i, gr, gi, a.twr, a.twi, a.kap, a.stretchx, lane, o2r, o2i);
+    __syncwarp();
+    const T *v0xk = a.v0x + (size_t)b * a.bg2 + ro;
+    for (int x = lane; x < nx; x += WARP) {
+        const T w = T(-2) * a.fsign * __ldg(v0xk + x);
+        a.FXX[(size_t)b * F + ro + x] = w * o2r[x];
+        a.FXZ[(size_t)b * F + ro + x] = w * o2i[x];
+    }
+}
+
+// Generic spectral x-derivative of nrows rows (two rows per warp).
+template <typename T, int N>
+__global__ void __launch_bounds__(ROW_WPB *WARP) ddx_kernel(const T *__restrict__ var, T *__restrict__ dvar,
+                                                              int nrows, T stretchx, const T *twr, const T *twi,
+                                                              const T *kap)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r0 = 2 * (blockIdx.x * ROW_WPB + warp);
+    if (r0 >= nrows) return;
+    const bool two = r0 + 1 < nrows;
+    T *xr = sm + warp * 4 * N, *xi = xr + N, *yr = xi + N, *yi = yr + N;
+    for (int x = lane; x < N; x += WARP) {
+        xr[x] = var[(size_t)r0 * N + x];
+        xi[x] = two ? var[(size_t)(r0 + 1) * N + x] : T(0);
+    }
+    __syncwarp();
+    T *orr, *oi;
+    fft_deriv<T, N>(xr, xi, yr, yi, twr, twi, kap, stretchx, lane, orr, oi);
+    __syncwarp();
+    for (int x = lane; x < N; x += WARP) {
+        dvar[(size_t)r0 * N + x] = orr[x];
+        if (two) dvar[(size_t)(r0 + 1) * N + x] = oi[x];
+    }
+}
+
+#define SPARC_FFT_SIZES(X) X(64) X(128) X(192) X(256) X(384) X(512) X(768) X(1024)
+
+bool fft_size_supported(int n)
+{
+#define CASE(n_) if (n == n_) return true;
+    SPARC_FFT_SIZES(CASE)
+#undef CASE
+    return false;
+}
+
+template <typename T, int N>
+static cudaError_t row_stage_n(const StepArgs<T> &a, cudaStream_t st)
+{
+    const int rows = a.nb * a.nz;
+    const int grid = (rows + ROW_WPB - 1) / ROW_WPB;
+    const size_t smem = (size_t)ROW_WPB * 4 * N * sizeof(T);
+    if (a.stage == 1) {
+        auto k = row_stage_kernel<T, N, 0>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, ROW_WPB * WARP, smem, st>>>(a);
+    } else if (a.stage <= 5) {
+        auto k = row_stage_kernel<T, N, 1>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, ROW_WPB * WARP, smem, st>>>(a);
+    } else {
+        auto k = row_stage_kernel<T, N, 2>;
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, ROW_WPB * WARP, smem, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_row_stage(const StepArgs<T> &a, cudaStream_t st)
+{
+#define CASE(n_) if (a.nx == n_) return row_stage_n<T, n_>(a, st);
+    SPARC_FFT_SIZES(CASE)
+#undef CASE
+    return cudaErrorInvalidValue;
+}
+
+template <typename T, int N>
+static cudaError_t ddx_n(const T *var, T *dvar, int nrows, T stretchx, const T *twr, const T *twi, const T *kap,
+                         cudaStream_t st)
+{
+    const int pairs = (nrows + 1) / 2;
+    const int grid = (pairs + ROW_WPB - 1) / ROW_WPB;
+    const size_t smem = (size_t)ROW_WPB * 4 * N * sizeof(T);
+    auto k = ddx_kernel<T, N>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<grid, ROW_WPB * WARP, smem, st>>>(var, dvar, nrows, stretchx, twr, twi, kap);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_ddx(const T *var, T *dvar, int nrows, int nx, T stretchx, const T *twr, const T *twi,
+                       const T *kap, cudaStream_t st)
+{
+    if (nrows <= 0) return cudaSuccess;
+#define CASE(n_) if (nx == n_) return ddx_n<T, n_>(var, dvar, nrows, stretchx, twr, twi, kap, st);
+    SPARC_FFT_SIZES(CASE)
+#undef CASE
+    return cudaErrorInvalidValue;
+}
+
+template cudaError_t launch_row_stage<float>(const StepArgs<float> &, cudaStream_t);
+template cudaError_t launch_row_stage<double>(const StepArgs<double> &, cudaStream_t);
+template cudaError_t launch_ddx<float>(const float *, float *, int, int, float, const float *, const float *,
+                                       const float *, cudaStream_t);
+template cudaError_t launch_ddx<double>(const double *, double *, int, int, double, const double *,
+                                        const double *, const double *, cudaStream_t);
+
+}  // namespace sparc

@@ -1,0 +1,78 @@
+"""The C-ABI library loads, exports every function include/*.h declares, and its FP64
+compact-derivative tables reproduce dbyd2.f (checked on the host, no GPU needed)."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from sparc_flows_gb300 import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(sparc_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    L = capi.lib()
+    names = header_functions()
+    assert "sparc_forward" in names and "sparc_plan_create" in names
+    for n in names:
+        assert hasattr(L, n), n
+        assert n in capi.SIGNATURES, n
+
+
+def test_plan_create_rejects_bad_config_without_gpu_work():
+    L = capi.lib()
+    cfg = capi.SparcConfig()
+    cfg.nx, cfg.nz, cfg.nbatch, cfg.precision = 500, 300, 1, 32  # 500 is not in the FFT table
+    cfg.npmlbot = cfg.npmltop = 10
+    cfg.npmlhor = 9
+    cfg.steps_out, cfg.k_inj, cfg.k_obs = 15, 100, 120
+    h = ctypes.c_void_p()
+    rc = L.sparc_plan_create(ctypes.byref(cfg), ctypes.byref(h))
+    assert rc == -2 and not h.value
+    assert b"nx" in L.sparc_last_error()
+    assert L.sparc_plan_create(None, ctypes.byref(h)) == -1
+
+
+@pytest.mark.parametrize("ibc", [0, 1, 2, 3])
+@pytest.mark.parametrize("lmax", [16, 32])
+def test_partitioned_tables_match_dbyd2(ibc, lmax):
+    rng = np.random.default_rng(10 * ibc + lmax)
+    nz, n1 = 300, 7
+    b = rng.standard_normal((nz, n1))
+    preset = rng.standard_normal(n1)
+    pre_full = np.zeros((nz, n1))
+    if ibc == 2:
+        pre_full[0] = preset
+    if ibc == 3:
+        pre_full[nz - 1] = preset
+    ref = O.dbyd2(b, ibc, preset=pre_full)
+    out = np.zeros((nz, n1))
+    dp = ctypes.POINTER(ctypes.c_double)
+    rc = capi.lib().sparc_zsolve_host(nz, ibc, lmax, b.ctypes.data_as(dp), out.ctypes.data_as(dp),
+                                      preset.ctypes.data_as(dp), n1)
+    assert rc == 0
+    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("nz", [64, 100, 301, 384])
+def test_partitioned_tables_other_depths(nz):
+    rng = np.random.default_rng(nz)
+    b = rng.standard_normal((nz, 3))
+    ref = O.dbyd2(b, 1)
+    out = np.zeros_like(b)
+    dp = ctypes.POINTER(ctypes.c_double)
+    rc = capi.lib().sparc_zsolve_host(nz, 1, 32, b.ctypes.data_as(dp), out.ctypes.data_as(dp), None, 3)
+    assert rc == 0
+    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
