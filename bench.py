@@ -1,0 +1,289 @@
+"""Benchmark of the wave-solver hot path: FP32 batched forward + adjoint + kernel accumulation.
+
+Workload (the batched FP32 configuration): 32 sources at x = -200 + 12.5 (s + 0.5) Mm over a
+400 Mm box, nx = 512, nz = 300 polytrope, supergranule stream-function flow (vx peak 240 m/s)
+and a 5 % Gaussian sound-speed bump, 3600 steps of 2 s, receivers every 2 Mm.  One bench step
+is one full forward solve (with partial states kept in HBM every 15 steps) plus one full
+adjoint solve with the kernel integral accumulated at every record, for all 32 sources.
+Metric: grid-point steps per second, forward and adjoint steps counted once each.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU restatement of the reference Fortran (the FP64 oracle; the
+Fortran itself cannot be built here) on all host cores, one solve per core, on a bounded
+sample of the same workload.  Under torchrun only rank 0 runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "batch32: 32 sources, nx=512 (400 Mm), nz=300 polytrope, psi flow 240 m/s + 5% c bump, 3600 steps"
+METRIC = "fwd+adj grid-pt-steps/s: FP32 batched vs FP64 plain, 1 GB300, <=1e-4 rel err"
+UNIT = "grid-pt-steps/s"
+
+
+def words_per_point_step(nx, nz, npmlbot=10, npmltop=10, npmlhor=9, V=4, B=3):
+    """Algorithmic words per grid-point step of the fused schedule: 15 V + 10 + 5 B + 15 Naux/N."""
+    naux = 2 * nx * (npmlbot + npmltop) + 2 * (2 * npmlhor) * nz
+    return 15 * V + 10 + 5 * B + 15 * naux / (nx * nz)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [v.strip() for v in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------------------------
+def run_reference(args):
+    """CPU arm: the FP64 oracle on all host cores, one solve per core (bounded sample)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import oracle as O
+    from sparc_flows_gb300 import model as M
+
+    run, model, specs, psi, cmul = M.workload("batch32")
+    cores = os.cpu_count() or 1
+    nsolve = min(cores, len(specs))
+    sample_steps = int(os.environ.get("SPARC_CPU_SAMPLE_STEPS", "40"))
+    xlocs = [s.xloc for s in specs[:nsolve]]
+    O.build()
+
+    def sample():
+        t0 = time.perf_counter()
+        O.run_batch(run.replace(nsteps=sample_steps), model, xlocs, psi, sample_steps, nsolve)
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        sample()
+    ts = [sample() for _ in range(args.steps)]
+    units = nsolve * run.nx * run.nz * sample_steps
+    value = units * len(ts) / sum(ts)
+    desc = (f"{nsolve} forward solves of the batch32 grid ({sample_steps} steps each, one per host thread); "
+            "adjoint steps cost the same per grid-point step")
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "higher_is_better": True,
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * sum(ts) / len(ts), "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": {"workload": WORKLOAD, "sample": desc},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": nsolve, "kind": "port", "sample": desc},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def cpu_baseline_quick():
+    """Bounded oracle sample for the gb300 line's cpu_baseline (~10-20 s)."""
+    from oracle import oracle as O
+    from sparc_flows_gb300 import model as M
+
+    run, model, specs, psi, cmul = M.workload("batch32")
+    cores = os.cpu_count() or 1
+    nsolve = min(cores, len(specs))
+    steps = int(os.environ.get("SPARC_CPU_SAMPLE_STEPS", "40"))
+    O.build()
+    t0 = time.perf_counter()
+    O.run_batch(run.replace(nsteps=steps), model, [s.xloc for s in specs[:nsolve]], psi, steps, nsolve)
+    dt = time.perf_counter() - t0
+    v = nsolve * run.nx * run.nz * steps / dt
+    return {"value": v, "unit": UNIT, "cores": nsolve, "kind": "port",
+            "sample": f"{nsolve} FP64 forward solves x {steps} steps of the batch32 grid on {nsolve} host threads"}
+
+
+# ----------------------------------------------------------------------------------------------
+def run_gpu(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from sparc_flows_gb300 import model as M
+    from sparc_flows_gb300.pipeline import FwdAdjKernels
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+
+    run, model, specs, psi, cmul = M.workload("batch32")
+    if args.nsteps:
+        run = run.replace(nsteps=args.nsteps)
+    pipe = FwdAdjKernels(run, model, specs, psi=psi, cmul=cmul, precision=32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        pipe.run_all()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            pipe.run_all()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    units = pipe.point_steps() * args.steps * world
+    value = units / (ms * 1e-3)
+
+    # ---- per-pass timing (CUDA events on the launching stream, outside the timed loop)
+    passes = pipe.fwd.profile_passes(nsteps=20)
+
+    # ---- end-to-end through the public API: pinned host inputs in, host kernels/seismograms out
+    nrec = run.nrec
+    data_h = torch.zeros((len(specs), nrec, run.nx), dtype=torch.float32).pin_memory()
+    psi_h = torch.as_tensor(psi, dtype=torch.float64).pin_memory()
+    kern_h = torch.empty((4, run.nz, run.nx), dtype=torch.float64).pin_memory()
+    seis_h = torch.empty((len(specs), nrec, run.nx), dtype=torch.float32).pin_memory()
+    h2d = data_h.numel() * 4 + psi_h.numel() * 8
+    d2h = kern_h.numel() * 8 + seis_h.numel() * 4
+    e2e_steps = max(1, min(args.steps, 2))
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        data_d = data_h.to(dev, non_blocking=True)
+        psi_d = psi_h.to(dev, non_blocking=True)
+        pipe.fwd.update_flow(psi_d)
+        pipe.adj.update_flow(psi_d)
+        seis, kacc = pipe.run_all(data_d)
+        kern_h.copy_(kacc.sum(0), non_blocking=True)
+        seis_h.copy_(seis, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    te = torch.tensor([e2e_ms], device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_ms = float(te.item())
+    e2e_value = pipe.point_steps() * e2e_steps * world / (e2e_ms * 1e-3)
+
+    if rank == 0:
+        words = words_per_point_step(run.nx, run.nz)
+        peak, peak_kind = measured_peak_hbm()
+        achieved = words * 4 * value / world / 1e9  # GB/s on one GPU
+        dom = max(passes["per_class_ms"], key=passes["per_class_ms"].get)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sources_per_gpu": len(specs), "nx": run.nx, "nz": run.nz,
+                       "nsteps": run.nsteps, "step": "forward + adjoint + kernel integral of all sources",
+                       "l2": "inputs larger than L2 (working set ~0.4 GB state + 28 GB partial states per GPU)",
+                       "parallelism": f"replicas x{world} (sources sharded, no collective)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "one RK time step (12 launches, CUDA graph)",
+                         "algorithmic_bytes_per_point_step": words * 4, "peak_kind": peak_kind,
+                         "dominant_kernel": dom, "pass_ms_per_step": passes["per_class_ms"],
+                         "pass_share": passes["share"]},
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": e2e_steps},
+            "gpu_launches": pipe.launch_count() * args.steps,
+        }
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline_quick()
+        print(json.dumps(line), flush=True)
+    pipe.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nsteps", type=int, default=0, help="override the 3600 time steps (testing only)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

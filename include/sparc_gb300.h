@@ -77,6 +77,11 @@ const char *sparc_last_error(void);
 int sparc_ddz(sparc_plan_t *plan, const double *var, double *dvar, int n1, int ibc,
               const double *preset, const double *stretch, void *stream);
 
+/* The kernel-stage z-derivative ddzkern (kernels.f90:648-661): sparc_ddz followed by the
+ * FILTER_VAR_Z smoothing of rows 2..nz-1 (kernels.f90:891-928).  FP64 device pointers. */
+int sparc_ddzkern(sparc_plan_t *plan, const double *var, double *dvar, int n1, int ibc,
+                  const double *stretch, void *stream);
+
 /* Spectral x-derivative of nrows rows of nx values (FP64, device pointers), times stretchx.
  * Replaces ddx (derivatives.f90:28-58). */
 int sparc_ddx(sparc_plan_t *plan, const double *var, double *dvar, int nrows, double stretchx,
@@ -113,6 +118,11 @@ int sparc_forward(sparc_plan_t *plan, int nsteps, double flow_sign, void *seis, 
 int sparc_get_state(sparc_plan_t *plan, void *dst, void *stream);
 int sparc_set_state(sparc_plan_t *plan, const void *src, void *stream);
 
+/* Timing of the passes of nsteps steps run without a graph, each launch bracketed by CUDA events
+ * on the given stream: ms[0] row passes, ms[1] column passes, ms[2] end-of-step passes,
+ * ms[3] wall time of the whole sequence (synchronises the stream; advances the state). */
+int sparc_profile_passes(sparc_plan_t *plan, int nsteps, double *ms, void *stream);
+
 /* Current step counter (synchronises the stream). */
 int sparc_get_time(sparc_plan_t *plan, int *time, void *stream);
 
@@ -125,6 +135,13 @@ int sparc_get_time(sparc_plan_t *plan, int *time, void *stream);
  * out is DEVICE FP64 [nbatch][4][nz][nx] (kc, kvx, kvz, hes), accumulated into. */
 int sparc_kernels(sparc_plan_t *plan, const void *fsn, int nfwd, const void *asn, int nadj,
                   int npair, double *out, void *stream);
+
+/* One record pair of the kernel integral with the plan's CURRENT state as the adjoint fields:
+ * forward record jf of fsn ([nbatch][nfwd][6][nz][nx], DEVICE, plan precision) pairs with the
+ * adjoint v_x, v_z of every solve as they stand now, accumulating into out as sparc_kernels does.
+ * Called after the adjoint step that produces a record, it replaces the adjoint partial-state
+ * dumps and their re-reading (all_modules.f90:750-784, kernels.f90:258-280). */
+int sparc_kernels_accumulate(sparc_plan_t *plan, const void *fsn, int nfwd, int jf, double *out, void *stream);
 
 /* Host-only FP64 evaluation of the partitioned compact-derivative algebra that the device
  * code applies (no GPU needed): x[nz][n1] = dbyd2(b, ibc) without the stretch factor, with

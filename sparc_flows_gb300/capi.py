@@ -25,6 +25,7 @@ SIGNATURES = {
     "sparc_plan_destroy": (ctypes.c_int, [_vp]),
     "sparc_last_error": (ctypes.c_char_p, []),
     "sparc_ddz": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    "sparc_ddzkern": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_ddx": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, ctypes.c_double, _vp]),
     "sparc_set_background": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_set_source": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _dp, _ip, ctypes.c_int, _vp]),
@@ -32,8 +33,10 @@ SIGNATURES = {
     "sparc_forward": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
     "sparc_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_set_state": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc_profile_passes": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _vp]),
     "sparc_get_time": (ctypes.c_int, [_vp, _ip, _vp]),
     "sparc_kernels": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
+    "sparc_kernels_accumulate": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_zsolve_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int]),
 }
 

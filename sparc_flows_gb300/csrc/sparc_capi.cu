@@ -414,6 +414,57 @@ cudaError_t enqueue_step(sparc_plan *p, StepArgs<T> a, cudaStream_t st)
 }
 
 template <typename T>
+int profile_passes(sparc_plan *p, int nsteps, double *ms, cudaStream_t st)
+{
+    StepArgs<T> a = solver<T>(p).a;
+    a.fsign = T(1);
+    a.seis = nullptr; a.snaps = nullptr; a.nrec_cap = 0;
+    a.unstretch_top = (T)p->unstretch_top;
+    const double *B = p->cfg.betas;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> cls;
+    auto rec = [&](int c) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        ev.push_back(e);
+        cls.push_back(c);
+    };
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < nsteps && e == cudaSuccess; i++) {
+        for (int s = 1; s <= 5 && e == cudaSuccess; s++) {
+            a.stage = s; a.bs = (T)B[s - 1]; a.bsm1 = (s >= 2) ? (T)B[s - 2] : T(0);
+            a.slot_s = s % 3; a.slot_sm1 = (s - 1) % 3; a.slot_sm2 = (s + 1) % 3;
+            rec(0); e = launch_row_stage<T>(a, st); rec(-1);
+            if (e != cudaSuccess) break;
+            rec(1); e = launch_col_stage<T>(a, st); rec(-1);
+        }
+        if (e != cudaSuccess) break;
+        a.stage = 6; a.bs = T(0); a.bsm1 = (T)B[4]; a.slot_s = 0; a.slot_sm1 = 2; a.slot_sm2 = 1;
+        rec(0); e = launch_row_stage<T>(a, st); rec(-1);
+        if (e != cudaSuccess) break;
+        a.stage = 7; a.bs = (T)B[4]; a.slot_s = 2; a.slot_sm1 = 1;
+        rec(2); e = launch_end_step<T>(a, st); rec(-1);
+    }
+    cudaError_t es = cudaStreamSynchronize(st);
+    ms[0] = ms[1] = ms[2] = ms[3] = 0.0;
+    if (e == cudaSuccess && es == cudaSuccess && ev.size() >= 2) {
+        for (size_t i = 0; i + 1 < ev.size(); i += 2) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+            ms[cls[i]] += t;
+        }
+        float tot = 0.f;
+        cudaEventElapsedTime(&tot, ev.front(), ev.back());
+        ms[3] = tot;
+    }
+    for (auto x : ev) cudaEventDestroy(x);
+    if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("profile: ") + cudaGetErrorString(e));
+    if (es != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("profile sync: ") + cudaGetErrorString(es));
+    return SPARC_OK;
+}
+
+template <typename T>
 int run_forward(sparc_plan *p, int nsteps, double fsign, void *seis, void *snaps, int cap, int use_graph,
                 cudaStream_t st)
 {
@@ -625,6 +676,16 @@ int sparc_ddz(sparc_plan_t *p, const double *var, double *dvar, int n1, int ibc,
     return SPARC_OK;
 }
 
+int sparc_ddzkern(sparc_plan_t *p, const double *var, double *dvar, int n1, int ibc, const double *stretch,
+                  void *stream)
+{
+    if (!p || !var || !dvar || n1 < 1) return fail(SPARC_ERR_ARG, "sparc_ddzkern: bad argument");
+    if (ibc < 0 || ibc > 1) return fail(SPARC_ERR_ARG, "sparc_ddzkern: ibc must be 0 or 1");
+    CK(launch_ddz<double>(p->z64[ibc].tab, p->nch64, p->L64, var, dvar, n1, p->cfg.nz, nullptr, stretch, 1,
+                          (cudaStream_t)stream));
+    return SPARC_OK;
+}
+
 int sparc_ddx(sparc_plan_t *p, const double *var, double *dvar, int nrows, double stretchx, void *stream)
 {
     if (!p || !var || !dvar || nrows < 0) return fail(SPARC_ERR_ARG, "sparc_ddx: bad argument");
@@ -667,6 +728,14 @@ int sparc_forward(sparc_plan_t *p, int nsteps, double flow_sign, void *seis, voi
                : run_forward<double>(p, nsteps, flow_sign, seis, snaps, nrec_cap, use_graph, (cudaStream_t)stream);
 }
 
+int sparc_profile_passes(sparc_plan_t *p, int nsteps, double *ms, void *stream)
+{
+    if (!p || !ms || nsteps < 1) return fail(SPARC_ERR_ARG, "sparc_profile_passes: bad argument");
+    if (!p->have_bg || !p->have_src) return fail(SPARC_ERR_STATE, "sparc_profile_passes: background and source first");
+    return p->cfg.precision == 32 ? profile_passes<float>(p, nsteps, ms, (cudaStream_t)stream)
+                                  : profile_passes<double>(p, nsteps, ms, (cudaStream_t)stream);
+}
+
 int sparc_get_state(sparc_plan_t *p, void *dst, void *stream)
 {
     if (!p || !dst) return fail(SPARC_ERR_ARG, "sparc_get_state: bad argument");
@@ -697,12 +766,71 @@ int sparc_get_time(sparc_plan_t *p, int *time, void *stream)
     return SPARC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+template <typename T>
+int kernels_impl(sparc_plan *p, const void *fsn, int nfwd, const void *adj, long long adj_stride, int jf, double *out,
+                 cudaStream_t st)
+{
+    Solver<T> &S = solver<T>(p);
+    const sparc_config_t &c = p->cfg;
+    const size_t F = S.F;
+    if (!S.work) {
+        void *ptr = nullptr;
+        CK(cudaMalloc(&ptr, (size_t)c.nbatch * 4 * F * sizeof(T)));
+        S.allocs.push_back(ptr);
+        S.work = (T *)ptr;
+    }
+    KAccArgs<T> k{};
+    k.nx = c.nx; k.nz = c.nz; k.nb = c.nbatch;
+    k.fsn = (const T *)fsn;
+    k.fbase = (long long)jf * 6 * F;
+    k.fstride = (long long)nfwd * 6 * F;
+    k.adj = (const T *)adj;
+    k.astride = adj_stride;
+    k.out = out;
+    k.work = S.work;
+    k.stretch = S.a.stretch;
+    k.twr = S.fft.twr; k.twi = S.fft.twi; k.kap = S.fft.kap;
+    k.stretchx = (T)c.stretchx;
+    k.z1 = S.z[1].tab;
+    k.nch = p->nch; k.L = p->L;
+    CK(launch_kacc<T>(k, st));
+    return SPARC_OK;
+}
+}  // namespace
+
+extern "C" {
+
 int sparc_kernels(sparc_plan_t *p, const void *fsn, int nfwd, const void *asn, int nadj, int npair, double *out,
                   void *stream)
 {
-    (void)fsn; (void)nfwd; (void)asn; (void)nadj; (void)npair; (void)out; (void)stream;
-    if (!p) return fail(SPARC_ERR_ARG, "sparc_kernels: null plan");
-    return fail(SPARC_ERR_STATE, "sparc_kernels: not available in this build");
+    if (!p || !fsn || !asn || !out || nfwd < 1 || nadj < 1 || npair < 0 || npair > nfwd || npair > nadj)
+        return fail(SPARC_ERR_ARG, "sparc_kernels: bad argument");
+    if (!p->have_bg) return fail(SPARC_ERR_STATE, "sparc_kernels: background must be set first");
+    const size_t F = (size_t)p->cfg.nx * p->cfg.nz;
+    const size_t es = p->cfg.precision == 32 ? 4 : 8;
+    for (int j = 0; j < npair; j++) {
+        const int ja = nadj - 1 - j;
+        const char *adj = (const char *)asn + ((size_t)ja * 6 * F + 2 * F) * es;
+        int rc = p->cfg.precision == 32
+                     ? kernels_impl<float>(p, fsn, nfwd, adj, (long long)nadj * 6 * F, j, out, (cudaStream_t)stream)
+                     : kernels_impl<double>(p, fsn, nfwd, adj, (long long)nadj * 6 * F, j, out, (cudaStream_t)stream);
+        if (rc != SPARC_OK) return rc;
+    }
+    return SPARC_OK;
+}
+
+int sparc_kernels_accumulate(sparc_plan_t *p, const void *fsn, int nfwd, int jf, double *out, void *stream)
+{
+    if (!p || !fsn || !out || nfwd < 1 || jf < 0 || jf >= nfwd)
+        return fail(SPARC_ERR_ARG, "sparc_kernels_accumulate: bad argument");
+    if (!p->have_bg) return fail(SPARC_ERR_STATE, "sparc_kernels_accumulate: background must be set first");
+    const size_t F = (size_t)p->cfg.nx * p->cfg.nz;
+    if (p->cfg.precision == 32)
+        return kernels_impl<float>(p, fsn, nfwd, p->s32.a.A + 2 * F, (long long)4 * F, jf, out, (cudaStream_t)stream);
+    return kernels_impl<double>(p, fsn, nfwd, p->s64.a.A + 2 * F, (long long)4 * F, jf, out, (cudaStream_t)stream);
 }
 
 // Host evaluation of the partitioned compact-derivative tables (FP64), the same algebra the

@@ -399,6 +399,109 @@ cudaError_t launch_ddz(const ZTab<T> &tb, int nch, int L, const T *var, T *dvar,
     return cudaGetLastError();
 }
 
+// Kernel integral, z-derivatives and FP64 accumulation of one record pair (kernels.f90:293-358):
+//   kc  += div(f_xi) div(a_v),  kvx += d_x f_vx a_vx + d_x f_vz a_vz,
+//   kvz += d_z f_vx a_vx + d_z f_vz a_vz,  hes += f_acc_x^2 + f_acc_z^2,
+// with every z-derivative taken as ddzkern (ibc 1, times stretch, then FILTER_VAR_Z,
+// kernels.f90:648-661, 891-928).  The x-derivatives come from kacc_row_kernel (work).
+template <typename T, int CW, int LMAX>
+__device__ __forceinline__ void kacc_dz(const KAccArgs<T> &a, const T *src, T *B0, T *B1, T *YB, int c, int j,
+                                        int x, int k0, int n, T (&out)[LMAX])
+{
+    const int nz = a.nz, nx = a.nx;
+    for (int m = 0; m < n; m++) B0[(k0 + m) * CW + c] = src[(size_t)(k0 + m) * nx + x];
+    __syncthreads();
+    T y[LMAX];
+    const T last = zlocal<T, LMAX>(a.z1, B0, CW, c, k0, n, nz, T(0), y);
+    YB[(2 * j) * CW + c] = y[0];
+    YB[(2 * j + 1) * CW + c] = last;
+    __syncthreads();
+    T xl, xr;
+    zcouple(a.z1, YB, CW, c, j, a.nch, xl, xr);
+#pragma unroll
+    for (int m = 0; m < LMAX; m++)
+        if (m < n) B1[(k0 + m) * CW + c] = zcorrect(a.z1, y[m], k0 + m, xl, xr) * __ldg(a.stretch + k0 + m);
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < LMAX; m++) {
+        if (m < n) {
+            const int k = k0 + m;
+            T v = B1[k * CW + c];
+            if ((k >= 1 && k <= 4) || (k >= nz - 5 && k <= nz - 2)) v = T(0.5) * (B1[(k + 1) * CW + c] + B1[(k - 1) * CW + c]);
+            else if (k >= 5 && k <= nz - 6) v = filt11(B1, CW, c, k);
+            out[m] = v;
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int CW, int LMAX>
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) kacc_col_kernel(KAccArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *B0 = reinterpret_cast<T *>(smem_raw);
+    const int nz = a.nz, nx = a.nx;
+    T *B1 = B0 + (size_t)nz * CW;
+    T *YB = B1 + (size_t)nz * CW;
+    const int c = threadIdx.x % CW, j = threadIdx.x / CW;
+    const int x = blockIdx.x * CW + c;
+    const int b = blockIdx.y;
+    const int k0 = j * a.L;
+    const int n = min(a.L, nz - k0);
+    const size_t F = (size_t)nz * nx;
+    const T *f = a.fsn + a.fbase + (size_t)b * a.fstride;
+    const T *avx = a.adj + (size_t)b * a.astride, *avz = avx + F;
+    const T *w = a.work + (size_t)b * 4 * F;
+    double *o = a.out + (size_t)b * 4 * F;
+    T divf[LMAX], d[LMAX];
+    kacc_dz<T, CW, LMAX>(a, f + 1 * F, B0, B1, YB, c, j, x, k0, n, divf);  // d_z f_xi_z
+#pragma unroll
+    for (int m = 0; m < LMAX; m++)
+        if (m < n) divf[m] += w[0 * F + (size_t)(k0 + m) * nx + x];
+    kacc_dz<T, CW, LMAX>(a, avz, B0, B1, YB, c, j, x, k0, n, d);  // d_z a_vz
+#pragma unroll
+    for (int m = 0; m < LMAX; m++) {
+        if (m < n) {
+            const size_t q = (size_t)(k0 + m) * nx + x;
+            const T diva = d[m] + w[1 * F + q];
+            o[0 * F + q] += (double)divf[m] * (double)diva;
+        }
+    }
+    kacc_dz<T, CW, LMAX>(a, f + 2 * F, B0, B1, YB, c, j, x, k0, n, divf);  // d_z f_vx
+    kacc_dz<T, CW, LMAX>(a, f + 3 * F, B0, B1, YB, c, j, x, k0, n, d);     // d_z f_vz
+#pragma unroll
+    for (int m = 0; m < LMAX; m++) {
+        if (m < n) {
+            const size_t q = (size_t)(k0 + m) * nx + x;
+            const double ax = (double)avx[q], az = (double)avz[q];
+            o[1 * F + q] += (double)w[2 * F + q] * ax + (double)w[3 * F + q] * az;
+            o[2 * F + q] += (double)divf[m] * ax + (double)d[m] * az;
+            const double fx = (double)f[4 * F + q], fz = (double)f[5 * F + q];
+            o[3 * F + q] += fz * fz + fx * fx;
+        }
+    }
+}
+
+template <typename T>
+cudaError_t launch_kacc_row(const KAccArgs<T> &a, cudaStream_t st);
+
+template <typename T>
+cudaError_t launch_kacc(const KAccArgs<T> &a, cudaStream_t st)
+{
+    constexpr int CW = ColCfg<T>::CW, LMAX = ColCfg<T>::LMAX;
+    if (a.nx % CW || a.L > LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
+    cudaError_t e = launch_kacc_row<T>(a, st);
+    if (e != cudaSuccess) return e;
+    const size_t smem = ((size_t)2 * a.nz * CW + (size_t)2 * a.nch * CW) * sizeof(T);
+    auto k = kacc_col_kernel<T, CW, LMAX>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid(a.nx / CW, a.nb);
+    k<<<grid, CW * a.nch, smem, st>>>(a);
+    return cudaGetLastError();
+}
+template cudaError_t launch_kacc<float>(const KAccArgs<float> &, cudaStream_t);
+template cudaError_t launch_kacc<double>(const KAccArgs<double> &, cudaStream_t);
+
 template cudaError_t launch_col_stage<float>(const StepArgs<float> &, cudaStream_t);
 template cudaError_t launch_col_stage<double>(const StepArgs<double> &, cudaStream_t);
 template cudaError_t launch_end_step<float>(const StepArgs<float> &, cudaStream_t);

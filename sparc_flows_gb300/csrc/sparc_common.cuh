@@ -272,9 +272,27 @@ cudaError_t launch_ddx(const T *var, T *dvar, int nrows, int nx, T stretchx, con
 template <typename T>
 cudaError_t launch_ddz(const ZTab<T> &tb, int nch, int L, const T *var, T *dvar, int n1, int nz,
                        const T *preset, const T *stretch, int filter, cudaStream_t st);
+// One forward/adjoint record pair of the kernel integral (kernels.f90:209-358).
+//   forward fields of solve b: fsn + fbase + b*fstride, six fields of F values each
+//                              (xi_x, xi_z, v_x, v_z, acc_x, acc_z);
+//   adjoint v_x of solve b:    adj + b*astride (v_z follows F values later);
+//   out [nb][4][nz][nx] FP64:  kc, kvx, kvz, hes;  work [nb][4][nz][nx] of T.
 template <typename T>
-cudaError_t launch_kernel_accum(const StepArgs<T> &a, const T *fsn, int nfwd, const T *asn, int nadj, int npair,
-                                double *out, T *work, cudaStream_t st);
+struct KAccArgs {
+    int nx, nz, nb;
+    const T *fsn;
+    long long fbase, fstride;
+    const T *adj;
+    long long astride;
+    double *out;
+    T *work;
+    const T *stretch, *twr, *twi, *kap;
+    T stretchx;
+    ZTab<T> z1;
+    int nch, L;
+};
+template <typename T>
+cudaError_t launch_kacc(const KAccArgs<T> &k, cudaStream_t st);
 
 bool fft_size_supported(int n);
 

@@ -213,6 +213,70 @@ cudaError_t launch_ddx(const T *var, T *dvar, int nrows, int nx, T stretchx, con
     return cudaErrorInvalidValue;
 }
 
+// Kernel integral, x-derivatives of one record pair: d/dx of forward xi_x, v_x, v_z and of the
+// adjoint v_x (compute_div / compute_del, kernels.f90:843-887).
+template <typename T, int N>
+__global__ void __launch_bounds__(ROW_WPB *WARP) kacc_row_kernel(KAccArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * ROW_WPB + warp;
+    if (row >= a.nb * a.nz) return;
+    T *xr = sm + warp * 4 * N, *xi = xr + N, *yr = xi + N, *yi = yr + N;
+    const int b = row / a.nz, k = row - b * a.nz;
+    const size_t F = (size_t)a.nz * N, ro = (size_t)k * N;
+    const T *f = a.fsn + a.fbase + (size_t)b * a.fstride;
+    const T *av = a.adj + (size_t)b * a.astride;
+    T *w = a.work + (size_t)b * 4 * F;
+    for (int x = lane; x < N; x += WARP) {
+        xr[x] = f[0 * F + ro + x];
+        xi[x] = av[ro + x];
+    }
+    __syncwarp();
+    T *o1r, *o1i;
+    fft_deriv<T, N>(xr, xi, yr, yi, a.twr, a.twi, a.kap, a.stretchx, lane, o1r, o1i);
+    __syncwarp();
+    for (int x = lane; x < N; x += WARP) {
+        w[0 * F + ro + x] = o1r[x];
+        w[1 * F + ro + x] = o1i[x];
+        o1r[x] = f[2 * F + ro + x];
+        o1i[x] = f[3 * F + ro + x];
+    }
+    __syncwarp();
+    T *gr = (o1r == xr) ? yr : xr, *gi = (o1r == xr) ? yi : xi;
+    T *o2r, *o2i;
+    fft_deriv<T, N>(o1r, o1i, gr, gi, a.twr, a.twi, a.kap, a.stretchx, lane, o2r, o2i);
+    __syncwarp();
+    for (int x = lane; x < N; x += WARP) {
+        w[2 * F + ro + x] = o2r[x];
+        w[3 * F + ro + x] = o2i[x];
+    }
+}
+
+template <typename T, int N>
+static cudaError_t kacc_row_n(const KAccArgs<T> &a, cudaStream_t st)
+{
+    const int rows = a.nb * a.nz;
+    const int grid = (rows + ROW_WPB - 1) / ROW_WPB;
+    const size_t smem = (size_t)ROW_WPB * 4 * N * sizeof(T);
+    auto k = kacc_row_kernel<T, N>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k<<<grid, ROW_WPB * WARP, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_kacc_row(const KAccArgs<T> &a, cudaStream_t st)
+{
+#define CASE(n_) if (a.nx == n_) return kacc_row_n<T, n_>(a, st);
+    SPARC_FFT_SIZES(CASE)
+#undef CASE
+    return cudaErrorInvalidValue;
+}
+template cudaError_t launch_kacc_row<float>(const KAccArgs<float> &, cudaStream_t);
+template cudaError_t launch_kacc_row<double>(const KAccArgs<double> &, cudaStream_t);
+
 template cudaError_t launch_row_stage<float>(const StepArgs<float> &, cudaStream_t);
 template cudaError_t launch_row_stage<double>(const StepArgs<double> &, cudaStream_t);
 template cudaError_t launch_ddx<float>(const float *, float *, int, int, float, const float *, const float *,

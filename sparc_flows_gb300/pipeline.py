@@ -1,0 +1,131 @@
+"""Forward solve, reference-style adjoint solve and sensitivity kernels for a batch of sources:
+the sequence full.py runs per source (full.py:18-59) -- ``sparc NN 00`` with the Spectral
+instruction, with the Adjoint instruction, then without one (kernel stage) -- done in one process
+with every wavefield resident in HBM instead of ~520 partial-state FITS dumps.
+
+Forward partial states are kept in device memory at the reference cadence (every
+steps_out steps, all_modules.f90:750-784).  The adjoint is the reference's continuous adjoint: a
+forward-type solve with the flow negated (driver.f90:144-147) driven by the time-reversed
+residual injected at o_rad (physics2d.f90:1052-1054).  After each adjoint step that produces a
+record, its v_x, v_z are paired with the matching forward record (kernels.f90:215, 258) and the
+kernel integrands are accumulated in FP64 on the device; the final scalings and the stream-function
+kernel follow kernels.f90:495-581.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from .config import DIMC, RSUN_CM, RunConfig
+from .model import SourceSpec
+from .solver import WaveSolver
+
+L1E8 = float(np.float32(1e-8))   # 10.0**(-8.) in kernels.f90 is a single-precision constant
+L1E5 = float(np.float32(1e-5))
+DIMRHO_KERNEL = float(np.float32(1e-3))  # kernel_back uses dimrho = 10.0**(-3.0) (initialize.f90:962)
+
+
+def receiver_columns(run: RunConfig, n: int = 128, x0: float = -127.0, dx: float = 2.0) -> np.ndarray:
+    """Grid columns nearest to receivers at x0 + dx*j Mm (box-centred coordinates)."""
+    x = (np.arange(run.nx) / run.nx - 0.5) * run.xlength_cm * 1e-8
+    return np.array([int(np.argmin(np.abs(x - (x0 + dx * j)))) for j in range(n)])
+
+
+class FwdAdjKernels:
+    """Batched forward + adjoint + kernel computation for one model and many sources."""
+
+    def __init__(self, run: RunConfig, model: np.ndarray, specs: list[SourceSpec], psi=None, cmul=None,
+                 precision: int = 32, receivers: np.ndarray | None = None, device: str = "cuda:0"):
+        self.run, self.nb = run, len(specs)
+        self.dev = torch.device(device)
+        self.fwd = WaveSolver(run, model, nbatch=self.nb, precision=precision, cmul=cmul, psi=psi, device=device)
+        self.fwd.set_forward_sources(specs)
+        self.adj = WaveSolver(run.replace(adjoint=True), model, nbatch=self.nb, precision=precision, cmul=cmul,
+                              psi=psi, device=device)
+        self.nrec = run.nrec
+        self.rcv = receiver_columns(run) if receivers is None else np.asarray(receivers)
+        dt = self.fwd.dtype
+        with torch.cuda.device(self.dev):
+            self.seis = torch.zeros((self.nb, self.nrec, run.nx), dtype=dt, device=self.dev)
+            self.snaps = torch.zeros((self.nb, self.nrec, 6, run.nz, run.nx), dtype=dt, device=self.dev)
+            self.kacc = torch.zeros((self.nb, 4, run.nz, run.nx), dtype=torch.float64, device=self.dev)
+            self.rcv_t = torch.as_tensor(self.rcv, device=self.dev)
+        self._adj_src = None
+
+    def adjoint_source(self, data: torch.Tensor | None) -> torch.Tensor:
+        """Waveform residual (synthetic minus data) at the receiver columns, time reversed, as the
+        adjoint source slices (nb, nrec, nx) at cadforcing cadence (the layout of source.fits)."""
+        res = self.seis.to(torch.float64)
+        if data is not None:
+            res = res - data.to(device=self.dev, dtype=torch.float64)
+        src = torch.zeros((self.nb, self.nrec, self.run.nx), dtype=torch.float64, device=self.dev)
+        src[:, :, self.rcv_t] = torch.flip(res[:, :, self.rcv_t], dims=[1])
+        return src
+
+    def forward(self):
+        self.fwd.reset(0)
+        self.fwd.run_steps(self.run.nsteps, self.seis, self.snaps, self.nrec)
+        return self.seis
+
+    def adjoint(self, src: torch.Tensor):
+        """Adjoint solve with kernel accumulation at each record (kernels.f90:209-358)."""
+        run, so = self.run, self.run.steps_out
+        self.adj.set_adjoint_sources_device(src)
+        self.adj.reset(0)
+        self.kacc.zero_()
+        done = 0
+        for ja in range(self.nrec):
+            n = 1 if ja == 0 else so
+            self.adj.run_steps(n, None, None, 0)
+            done += n
+            self.adj.kernels_accumulate(self.snaps, self.nrec - 1 - ja, self.kacc)
+        if run.nsteps > done:
+            self.adj.run_steps(run.nsteps - done, None, None, 0)
+
+    def run_all(self, data: torch.Tensor | None = None):
+        self.forward()
+        src = self.adjoint_source(data)
+        self.adjoint(src)
+        return self.seis, self.kacc
+
+    def launch_count(self) -> int:
+        """Kernels of ours launched by one run_all."""
+        per = WaveSolver.LAUNCHES_PER_STEP
+        return 2 * per * self.run.nsteps + 2 * self.nrec + 4
+
+    def point_steps(self) -> int:
+        """Grid-point steps of one run_all (forward and adjoint counted once each)."""
+        return 2 * self.nb * self.run.nx * self.run.nz * self.run.nsteps
+
+    def final_kernels(self, summed: bool = True) -> dict:
+        """Scaled kernels (kernels.f90:495-581): kernel_c, kernel_vx, kernel_vz, kernel_psi, hessian."""
+        run = self.run
+        acc = self.kacc.sum(0, keepdim=True) if summed else self.kacc
+        nz, nx = run.nz, run.nx
+        rho0k = torch.as_tensor(self.fwd.rho0 * 1e-3 / DIMRHO_KERNEL, device=self.dev)[None, :, None]
+        c2k = torch.as_tensor(np.stack(self.fwd.c2), device=self.dev)
+        c2k = c2k[:1] if summed or c2k.shape[0] == 1 else c2k
+        stepskern = float(run.steps_out)
+        dimen = 1.0 / (RSUN_CM * L1E8 * run.xlength_cm * L1E8 * DIMC * L1E5)
+        kv1, kv3 = acc[:, 1], acc[:, 2]
+        t2 = torch.empty((nz, nx), dtype=torch.float64, device=self.dev)
+        t3 = torch.empty_like(t2)
+        kpsi = torch.empty_like(kv1)
+        for b in range(acc.shape[0]):
+            self.fwd.ddzkern(kv1[b].contiguous(), t2, n1=nx, ibc=0, stretch=self.fwd.stretch_t)
+            self.fwd.ddx(kv3[b].contiguous(), t3, nrows=nz, stretchx=self.fwd.stretchx)
+            kpsi[b] = t2 - t3
+        fac = stepskern * run.timestep
+        kernel_psi = 2.0 * kpsi * dimen * (rho0k * torch.sqrt(c2k)) * fac * dimen
+        kernel_vx = -2.0 * kv1 * rho0k * fac * dimen
+        kernel_vz = -2.0 * kv3 * rho0k * fac * dimen
+        dimc2 = 1.0 / (RSUN_CM * L1E8 * run.xlength_cm * L1E8)
+        kernel_c = -acc[:, 0] * rho0k * c2k * fac * dimc2 * 2.0
+        return dict(kernel_c=kernel_c, kernel_vx=kernel_vx, kernel_vz=kernel_vz, kernel_psi=kernel_psi,
+                    hessian=acc[:, 3])
+
+    def close(self):
+        self.fwd.close()
+        self.adj.close()

@@ -225,6 +225,11 @@ class WaveSolver:
         capi.check(self.L.sparc_ddz(self.plan, _ptr(var), _ptr(dvar), n1, ibc, _ptr(preset), _ptr(stretch),
                                     _stream()), "sparc_ddz")
 
+    def ddzkern(self, var: torch.Tensor, dvar: torch.Tensor, n1: int, ibc: int, stretch=None):
+        """FP64 kernel-stage z-derivative with FILTER_VAR_Z (ddzkern, kernels.f90:648-661)."""
+        capi.check(self.L.sparc_ddzkern(self.plan, _ptr(var), _ptr(dvar), n1, ibc, _ptr(stretch), _stream()),
+                   "sparc_ddzkern")
+
     def ddx(self, var: torch.Tensor, dvar: torch.Tensor, nrows: int, stretchx: float):
         """FP64 spectral x-derivative of nrows rows (ddx, derivatives.f90:28-58)."""
         capi.check(self.L.sparc_ddx(self.plan, _ptr(var), _ptr(dvar), nrows, stretchx, _stream()), "sparc_ddx")
@@ -257,10 +262,20 @@ class WaveSolver:
         idx, w = lagrange_weights(self.run, ntab, self.run.num_steps, src.shape[1])
         self._set_source(src, w, idx)
 
+    def set_adjoint_sources_device(self, src: torch.Tensor):
+        """As set_adjoint_sources, with the slices already on the device (FP64)."""
+        if src.dim() != 3 or src.shape[0] != self.nb or src.shape[2] != self.run.nx:
+            raise ValueError("adjoint source must be (nbatch, nt, nx)")
+        if getattr(self, "_lagr", None) is None or self._lagr[0] != src.shape[1]:
+            idx, w = lagrange_weights(self.run, self.run.nsteps, self.run.num_steps, src.shape[1])
+            self._lagr = (src.shape[1], idx, w)
+        _, idx, w = self._lagr
+        self._set_source(src, w, idx)
+
     def _set_source(self, rows, wts, idx):
         inj = np.broadcast_to(self.delta_width / self.rho0[self.k_inj], (self.nb, self.run.nx))
         inj_t = self._t(inj)
-        rows_t = self._t(rows)
+        rows_t = rows.to(torch.float64).contiguous() if isinstance(rows, torch.Tensor) else self._t(rows)
         w = np.ascontiguousarray(wts, dtype=np.float64)
         ix = np.ascontiguousarray(idx, dtype=np.int32)
         capi.check(self.L.sparc_set_source(self.plan, _ptr(inj_t), _ptr(rows_t), rows.shape[1],
@@ -268,6 +283,34 @@ class WaveSolver:
                                            ix.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(ix), _stream()),
                    "sparc_set_source")
         torch.cuda.synchronize(self.dev)
+
+    def update_flow(self, psi: torch.Tensor):
+        """New stream function (nz, nx) in Mm, a device tensor: recompute v0 on the GPU
+        (driver.f90:94-115) and upload it; the rest of the background is kept."""
+        run, nx, nz = self.run, self.run.nx, self.run.nz
+        if not self.flows or self.nbg != 1:
+            raise ValueError("update_flow needs a flow-enabled solver with one shared background")
+        psi = psi.to(device=self.dev, dtype=torch.float64).reshape(nz, nx)
+        r0 = self.bg["rho0"][:, None]
+        c = torch.sqrt(torch.as_tensor(self.c2[0], device=self.dev))
+        pv = (r0 * c * (psi / (RSUN_CM / 1.0e8))).contiguous()
+        v0x = torch.empty((1, nz, nx), dtype=torch.float64, device=self.dev)
+        v0z = torch.empty_like(v0x)
+        self.ddz(pv, v0x[0], n1=nx, ibc=1, stretch=self.stretch_t)
+        self.ddx(pv, v0z[0], nrows=nz, stretchx=self.stretchx)
+        self.bg["v0x"] = (-v0x / r0[None]).contiguous()
+        self.bg["v0z"] = (v0z / r0[None]).contiguous()
+        self.v0x, self.v0z = self.bg["v0x"], self.bg["v0z"]
+        bgs = capi.SparcBackground()
+        for name, t in self.bg.items():
+            setattr(bgs, name, t.data_ptr() if t is not None else None)
+        capi.check(self.L.sparc_set_background(self.plan, ctypes.byref(bgs), _stream()), "sparc_set_background")
+
+    def kernels_accumulate(self, fsnaps: torch.Tensor, jf: int, out: torch.Tensor):
+        """Accumulate the kernel integrand of forward record jf against this solver's current
+        state (the adjoint fields) into out (nb, 4, nz, nx) FP64."""
+        capi.check(self.L.sparc_kernels_accumulate(self.plan, _ptr(fsnaps), fsnaps.shape[1], jf, _ptr(out),
+                                                   _stream()), "sparc_kernels_accumulate")
 
     def reset(self, time0: int = 0):
         capi.check(self.L.sparc_reset_state(self.plan, time0, _stream()), "sparc_reset_state")
@@ -305,6 +348,18 @@ class WaveSolver:
     def set_state(self, st: torch.Tensor):
         st = st.to(device=self.dev, dtype=self.dtype).contiguous()
         capi.check(self.L.sparc_set_state(self.plan, _ptr(st), _stream()), "sparc_set_state")
+
+    def profile_passes(self, nsteps: int = 20) -> dict:
+        """Event-timed passes of nsteps steps (no graph): milliseconds per step by pass class.
+        Advances the state; call reset() before a real run."""
+        ms = (ctypes.c_double * 4)()
+        capi.check(self.L.sparc_profile_passes(self.plan, nsteps, ms, _stream()), "sparc_profile_passes")
+        per = {"row": ms[0] / nsteps, "column": ms[1] / nsteps, "end": ms[2] / nsteps}
+        tot = sum(per.values())
+        return {"per_class_ms": per, "share": {k: v / tot for k, v in per.items()} if tot > 0 else {},
+                "wall_ms_per_step": ms[3] / nsteps}
+
+    LAUNCHES_PER_STEP = 12  # 6 row passes, 5 column passes, 1 end-of-step pass
 
     def time(self) -> int:
         t = ctypes.c_int()
