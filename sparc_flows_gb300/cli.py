@@ -1,0 +1,186 @@
+"""``sparc NN MM`` drop-in for the reference executable (driver.f90:1-331, READ_PARAMETERS
+initialize.f90:984-1144), backed by the GPU solver.
+
+Callers (data_forward.py:15-18, full.py:18-59, linesearch.py:16-19) run
+``mpiexec -np 1 ./sparc NN MM`` in the code directory and check the exit status.  The mode is
+chosen exactly as in READ_PARAMETERS:
+  Instruction_srcNN_lsMM line 1 'spectral' -> forward solve (the instruction file is removed,
+                                              driver.f90:243);
+  line 1 'adjoint'                         -> adjoint solve;
+  no instruction file                      -> kernel construction (PRODUCE_KERNELS).
+Marker files in the working directory: compute_data, linesearch, compute_synth.
+
+Files written (same names and FITS layout as the reference):
+  <dir>/forward_srcNN_lsMM/{vz_cc.fits, timeline, kernel_info, rms_hist}
+  <dir>/adjoint_srcNN/{kernel_info, timeline, rms_hist}
+  <dir>/kernel/{kernel_c_NN, kernel_vx_NN, kernel_vz_NN, kernel_psi_NN, hessian_NN}.fits
+The partial states the reference dumps every 15 steps as ~3000 FITS files
+(all_modules.f90:750-784) are kept as one array file per run (partial_states.npy) in the same
+folders and removed by the kernel stage, as PRODUCE_KERNELS removes its *partial* files.
+
+Adjoint source: the travel-time adjoint source of ADJOINT_SOURCE_FILT (driver.f90:1758-2238) is
+not part of this build; a forward run that is not a data run writes a waveform adjoint source
+(time-reversed synthetic minus <dir>/data/NN.fits at every column) to adjoint_srcNN/source.fits.
+
+Environment: SPARC_PRECISION (64, or 32), SPARC_DEVICE (cuda:0), SPARC_NSTEPS (override maxtime+1).
+"""
+from __future__ import annotations
+
+import math
+import os
+import sys
+
+import numpy as np
+
+from . import fits
+from .config import DIMC, parse_params_i, run_config_from_params
+from .model import SourceSpec, load_model, SPATIAL_REFERENCE, TEMPORAL_REFERENCE
+
+
+def _read_instruction(path):
+    with open(path) as f:
+        lines = [ln.strip() for ln in f.read().splitlines()]
+    kind = lines[0].strip().lower() if lines else ""
+    twod = len(lines) > 1 and lines[1].strip().upper() == "2D"
+    return kind, twod
+
+
+def _master_pixel(directory, src):
+    with open(os.path.join(directory, "master.pixels")) as f:
+        vals = [float(ln.split()[0]) for ln in f if ln.strip()][:100]
+    if src < 1 or src > len(vals):
+        raise SystemExit(f"sparc: source {src} not in master.pixels ({len(vals)} entries)")
+    return vals[src - 1]
+
+
+def main(argv=None) -> int:
+    argv = list(sys.argv[1:] if argv is None else argv)
+    if len(argv) < 2:
+        print("usage: sparc <src NN> <job MM>", file=sys.stderr)
+        return 2
+    contrib, jobno = argv[0], argv[1]
+    src = int(contrib)
+    params = parse_params_i(open("params.i").read())
+    directory = params["directory"]
+    run = run_config_from_params(params)
+    if os.environ.get("SPARC_NSTEPS"):
+        run = run.replace(nsteps=int(os.environ["SPARC_NSTEPS"]))
+    precision = int(os.environ.get("SPARC_PRECISION", "64"))
+    device = os.environ.get("SPARC_DEVICE", "cuda:0")
+    model = load_model(params.get("file_data", "solar_deep"), run.nz)
+    instr = f"Instruction_src{contrib}_ls{jobno}"
+    compute_data = os.path.exists("compute_data")
+    if os.path.exists(instr):
+        kind, _ = _read_instruction(instr)
+        if kind == "spectral":
+            rc = _forward(run, model, directory, contrib, jobno, src, precision, device, compute_data)
+            if os.path.exists(instr):
+                os.remove(instr)
+            return rc
+        if kind == "adjoint":
+            return _adjoint(run, model, directory, contrib, jobno, precision, device)
+        print(f"sparc: unknown instruction {kind!r}", file=sys.stderr)
+        return 2
+    return _kernels(run, model, directory, contrib, jobno, precision, device)
+
+
+def _flow_inputs(run, directory, jobno, compute_data):
+    """Stream function or direct flow (driver.f90:63-147)."""
+    if not run.flows:
+        return None, None
+    if compute_data and os.path.exists("true_vx.fits"):
+        vx = fits.read("true_vx.fits").reshape(run.nz, run.nx) * 1e2 / DIMC
+        vz = fits.read("true_vz.fits").reshape(run.nz, run.nx) * 1e2 / DIMC
+        return None, (vx, vz)
+    p = os.path.join(directory, f"model_psi_ls{jobno}.fits")
+    if os.path.exists(p):
+        return fits.read(p).reshape(run.nz, run.nx), None
+    return None, None
+
+
+def _solver(run, model, directory, jobno, precision, device, compute_data, nb=1):
+    import torch
+    from .solver import WaveSolver
+
+    psi, direct = _flow_inputs(run, directory, jobno, compute_data)
+    ws = WaveSolver(run, model, nbatch=nb, precision=precision, psi=psi, device=device)
+    if direct is not None:
+        ws.set_flow_direct(torch.as_tensor(direct[0]), torch.as_tensor(direct[1]))
+    return ws
+
+
+def _forward(run, model, directory, contrib, jobno, src, precision, device, compute_data):
+    import torch
+
+    out = os.path.join(directory, f"forward_src{contrib}_ls{jobno}")
+    os.makedirs(out, exist_ok=True)
+    xloc = _master_pixel(directory, src)
+    ws = _solver(run, model, directory, jobno, precision, device, compute_data)
+    ws.set_forward_sources([SourceSpec(xloc, SPATIAL_REFERENCE, 0.5, TEMPORAL_REFERENCE, 0.003)])
+    keep = not (os.path.exists("compute_synth") or os.path.exists("linesearch") or compute_data)
+    res = ws.forward(snapshots=keep)
+    seis, snaps = (res if keep else (res, None))
+    s = seis.double().cpu().numpy()[0]
+    fits.write(os.path.join(out, "vz_cc.fits"), s[:, None, :])
+    with open(os.path.join(out, "kernel_info"), "w") as f:
+        f.write(f"{0}\n{run.nsteps - 1}\n")
+    with open(os.path.join(out, "timeline"), "w") as f:
+        for i in range(0, run.nsteps, run.steps_out):
+            f.write(f"{i} {-run.solartime_h * 3600.0 + (i + 1) * run.timestep}\n")
+    with open(os.path.join(out, "rms_hist"), "w") as f:
+        f.write(f"{float(np.sqrt((s[-1] ** 2).sum()))}\n")
+    if keep:
+        np.save(os.path.join(out, "partial_states.npy"), snaps.cpu().numpy()[0])
+    if not compute_data:
+        data_p = os.path.join(directory, "data", f"{contrib}.fits")
+        adir = os.path.join(directory, f"adjoint_src{contrib}")
+        os.makedirs(adir, exist_ok=True)
+        data = fits.read(data_p).reshape(s.shape) if os.path.exists(data_p) else np.zeros_like(s)
+        fits.write(os.path.join(adir, "source.fits"), (s - data)[::-1][:, None, :])
+    ws.close()
+    return 0
+
+
+def _adjoint(run, model, directory, contrib, jobno, precision, device):
+    adir = os.path.join(directory, f"adjoint_src{contrib}")
+    srcf = os.path.join(adir, "source.fits")
+    if not os.path.exists(srcf):
+        print(f"sparc: missing {srcf}", file=sys.stderr)
+        return 1
+    arun = run.replace(adjoint=True)
+    ws = _solver(arun, model, directory, jobno, precision, device, False)
+    vr = fits.read(srcf).reshape(-1, run.nx)[: run.forcing_length]
+    ws.set_adjoint_sources(vr[None])
+    _, snaps = ws.forward(snapshots=True)
+    np.save(os.path.join(adir, "partial_states.npy"), snaps.cpu().numpy()[0])
+    with open(os.path.join(adir, "kernel_info"), "w") as f:
+        f.write(f"{run.forcing_length}\n{((run.nsteps - 1) // run.cadforcing_step) * run.cadforcing_step}\n")
+    ws.close()
+    return 0
+
+
+def _kernels(run, model, directory, contrib, jobno, precision, device):
+    import torch
+
+    from .pipeline import kernels_from_partial_states
+
+    fdir = os.path.join(directory, f"forward_src{contrib}_ls{jobno}")
+    adir = os.path.join(directory, f"adjoint_src{contrib}")
+    fp, ap = os.path.join(fdir, "partial_states.npy"), os.path.join(adir, "partial_states.npy")
+    if not (os.path.exists(fp) and os.path.exists(ap)):
+        print("sparc: partial states of the forward and adjoint runs are missing", file=sys.stderr)
+        return 1
+    ws = _solver(run, model, directory, jobno, precision, device, False)
+    ker = kernels_from_partial_states(ws, np.load(fp), np.load(ap))
+    kdir = os.path.join(directory, "kernel")
+    os.makedirs(kdir, exist_ok=True)
+    for name in ("kernel_c", "kernel_vx", "kernel_vz", "kernel_psi", "hessian"):
+        fits.write(os.path.join(kdir, f"{name}_{contrib}.fits"), ker[name][:, None, :])
+    os.remove(fp)
+    os.remove(ap)
+    ws.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -101,31 +101,59 @@ class FwdAdjKernels:
 
     def final_kernels(self, summed: bool = True) -> dict:
         """Scaled kernels (kernels.f90:495-581): kernel_c, kernel_vx, kernel_vz, kernel_psi, hessian."""
-        run = self.run
         acc = self.kacc.sum(0, keepdim=True) if summed else self.kacc
-        nz, nx = run.nz, run.nx
-        rho0k = torch.as_tensor(self.fwd.rho0 * 1e-3 / DIMRHO_KERNEL, device=self.dev)[None, :, None]
-        c2k = torch.as_tensor(np.stack(self.fwd.c2), device=self.dev)
-        c2k = c2k[:1] if summed or c2k.shape[0] == 1 else c2k
-        stepskern = float(run.steps_out)
-        dimen = 1.0 / (RSUN_CM * L1E8 * run.xlength_cm * L1E8 * DIMC * L1E5)
-        kv1, kv3 = acc[:, 1], acc[:, 2]
-        t2 = torch.empty((nz, nx), dtype=torch.float64, device=self.dev)
-        t3 = torch.empty_like(t2)
-        kpsi = torch.empty_like(kv1)
-        for b in range(acc.shape[0]):
-            self.fwd.ddzkern(kv1[b].contiguous(), t2, n1=nx, ibc=0, stretch=self.fwd.stretch_t)
-            self.fwd.ddx(kv3[b].contiguous(), t3, nrows=nz, stretchx=self.fwd.stretchx)
-            kpsi[b] = t2 - t3
-        fac = stepskern * run.timestep
-        kernel_psi = 2.0 * kpsi * dimen * (rho0k * torch.sqrt(c2k)) * fac * dimen
-        kernel_vx = -2.0 * kv1 * rho0k * fac * dimen
-        kernel_vz = -2.0 * kv3 * rho0k * fac * dimen
-        dimc2 = 1.0 / (RSUN_CM * L1E8 * run.xlength_cm * L1E8)
-        kernel_c = -acc[:, 0] * rho0k * c2k * fac * dimc2 * 2.0
-        return dict(kernel_c=kernel_c, kernel_vx=kernel_vx, kernel_vz=kernel_vz, kernel_psi=kernel_psi,
-                    hessian=acc[:, 3])
+        return scale_kernels(self.fwd, acc)
 
     def close(self):
         self.fwd.close()
         self.adj.close()
+
+
+def scale_kernels(ws: WaveSolver, acc: torch.Tensor) -> dict:
+    """Final scalings of PRODUCE_KERNELS (kernels.f90:495-581) applied to accumulated integrands
+    acc (n, 4, nz, nx) = (div f_xi div a_v, d_x f_v . a_v, d_z f_v . a_v, |f_acc|^2) summed over
+    the records.  The stream-function kernel is the y-component of the curl of the flow kernel
+    with the kernel-stage z-derivative at ibc 0 (CURL_KERN, kernels.f90:815-838, 510-513)."""
+    run, dev = ws.run, ws.dev
+    nz, nx = run.nz, run.nx
+    rho0k = torch.as_tensor(ws.rho0 * 1e-3 / DIMRHO_KERNEL, device=dev)[None, :, None]
+    c2k = torch.as_tensor(np.stack(ws.c2), device=dev)
+    if c2k.shape[0] != acc.shape[0]:
+        c2k = c2k[:1]
+    stepskern = float(run.steps_out)
+    dimen = 1.0 / (RSUN_CM * L1E8 * run.xlength_cm * L1E8 * DIMC * L1E5)
+    kv1, kv3 = acc[:, 1], acc[:, 2]
+    t2 = torch.empty((nz, nx), dtype=torch.float64, device=dev)
+    t3 = torch.empty_like(t2)
+    kpsi = torch.empty_like(kv1)
+    for b in range(acc.shape[0]):
+        ws.ddzkern(kv1[b].contiguous(), t2, n1=nx, ibc=0, stretch=ws.stretch_t)
+        ws.ddx(kv3[b].contiguous(), t3, nrows=nz, stretchx=ws.stretchx)
+        kpsi[b] = t2 - t3
+    fac = stepskern * run.timestep
+    kernel_psi = 2.0 * kpsi * dimen * (rho0k * torch.sqrt(c2k)) * fac * dimen
+    kernel_vx = -2.0 * kv1 * rho0k * fac * dimen
+    kernel_vz = -2.0 * kv3 * rho0k * fac * dimen
+    dimc2 = 1.0 / (RSUN_CM * L1E8 * run.xlength_cm * L1E8)
+    kernel_c = -acc[:, 0] * rho0k * c2k * fac * dimc2 * 2.0
+    return dict(kernel_c=kernel_c, kernel_vx=kernel_vx, kernel_vz=kernel_vz, kernel_psi=kernel_psi,
+                hessian=acc[:, 3])
+
+
+def kernels_from_partial_states(ws: WaveSolver, fsn: np.ndarray, asn: np.ndarray) -> dict:
+    """PRODUCE_KERNELS from stored partial states of one forward and one adjoint run
+    ((nrec, 6, nz, nx) each): pairs forward record j with adjoint record n-1-j and returns the
+    scaled kernels as (nz, nx) host arrays."""
+    import ctypes
+    from . import capi
+    from .solver import _ptr, _stream
+
+    dev, dt = ws.dev, ws.dtype
+    f = torch.as_tensor(fsn, dtype=dt, device=dev)[None].contiguous()
+    a = torch.as_tensor(asn, dtype=dt, device=dev)[None].contiguous()
+    npair = min(f.shape[1], a.shape[1])
+    acc = torch.zeros((1, 4, ws.run.nz, ws.run.nx), dtype=torch.float64, device=dev)
+    capi.check(ws.L.sparc_kernels(ws.plan, _ptr(f), f.shape[1], _ptr(a), a.shape[1], npair, _ptr(acc), _stream()),
+               "sparc_kernels")
+    out = scale_kernels(ws, acc)
+    return {k: v[0].cpu().numpy() for k, v in out.items()}

@@ -301,6 +301,20 @@ class WaveSolver:
         self.bg["v0x"] = (-v0x / r0[None]).contiguous()
         self.bg["v0z"] = (v0z / r0[None]).contiguous()
         self.v0x, self.v0z = self.bg["v0x"], self.bg["v0z"]
+        self._upload_background()
+
+    def set_flow_direct(self, v0x, v0z):
+        """Flow given directly (nondimensional, (nz, nx)), as the data run reads true_vx/true_vz
+        (driver.f90:63-76)."""
+        if not self.flows or self.nbg != 1:
+            raise ValueError("set_flow_direct needs a flow-enabled solver with one shared background")
+        nz, nx = self.run.nz, self.run.nx
+        self.bg["v0x"] = torch.as_tensor(v0x, dtype=torch.float64, device=self.dev).reshape(1, nz, nx).contiguous()
+        self.bg["v0z"] = torch.as_tensor(v0z, dtype=torch.float64, device=self.dev).reshape(1, nz, nx).contiguous()
+        self.v0x, self.v0z = self.bg["v0x"], self.bg["v0z"]
+        self._upload_background()
+
+    def _upload_background(self):
         bgs = capi.SparcBackground()
         for name, t in self.bg.items():
             setattr(bgs, name, t.data_ptr() if t is not None else None)
