@@ -123,6 +123,11 @@ int sparc_set_state(sparc_plan_t *plan, const void *src, void *stream);
  * ms[3] wall time of the whole sequence (synchronises the stream; advances the state). */
 int sparc_profile_passes(sparc_plan_t *plan, int nsteps, double *ms, void *stream);
 
+/* L2 norm of v_z of every solve, sqrt(sum a(:,:,:,6)^2) (the per-step rms_hist monitor of
+ * TIMESTEPPING, driver.f90:364-383), into norms[nbatch] (host).  Returns SPARC_ERR_NONFINITE if
+ * any norm is not finite (a diverged solve).  Synchronises the stream. */
+int sparc_check_state(sparc_plan_t *plan, double *norms, void *stream);
+
 /* Current step counter (synchronises the stream). */
 int sparc_get_time(sparc_plan_t *plan, int *time, void *stream);
 

@@ -34,6 +34,7 @@ SIGNATURES = {
     "sparc_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_set_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_profile_passes": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _vp]),
+    "sparc_check_state": (ctypes.c_int, [_vp, _dp, _vp]),
     "sparc_get_time": (ctypes.c_int, [_vp, _ip, _vp]),
     "sparc_kernels": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_kernels_accumulate": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),

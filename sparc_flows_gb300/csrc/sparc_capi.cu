@@ -216,6 +216,26 @@ cudaError_t cast_to(const double *src, T *dst, size_t n, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// Sum of squares of v_z per solve (one block per solve), FP64 accumulation.
+template <typename T>
+__global__ void vz_norm_kernel(const T *__restrict__ A, size_t F, double *__restrict__ out)
+{
+    const T *vz = A + ((size_t)blockIdx.x * 4 + 3) * F;
+    double s = 0.0;
+    for (size_t i = threadIdx.x; i < F; i += blockDim.x) {
+        const double v = (double)vz[i];
+        s += v * v;
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
 template <typename T>
 struct DevZ {
     T *buf = nullptr;
@@ -753,6 +773,30 @@ int sparc_set_state(sparc_plan_t *p, const void *src, void *stream)
     void *dst = p->cfg.precision == 32 ? (void *)p->s32.a.A : (void *)p->s64.a.A;
     CK(cudaMemcpyAsync(dst, src, (size_t)p->cfg.nbatch * 4 * p->cfg.nx * p->cfg.nz * es, cudaMemcpyDeviceToDevice,
                        (cudaStream_t)stream));
+    return SPARC_OK;
+}
+
+int sparc_check_state(sparc_plan_t *p, double *norms, void *stream)
+{
+    if (!p || !norms) return fail(SPARC_ERR_ARG, "sparc_check_state: bad argument");
+    const int nb = p->cfg.nbatch;
+    const size_t F = (size_t)p->cfg.nx * p->cfg.nz;
+    cudaStream_t st = (cudaStream_t)stream;
+    double *d = nullptr;
+    CK(cudaMallocAsync((void **)&d, nb * sizeof(double), st));
+    if (p->cfg.precision == 32) vz_norm_kernel<float><<<nb, 256, 0, st>>>(p->s32.a.A, F, d);
+    else vz_norm_kernel<double><<<nb, 256, 0, st>>>(p->s64.a.A, F, d);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(norms, d, nb * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("sparc_check_state: ") + cudaGetErrorString(e));
+    bool bad = false;
+    for (int b = 0; b < nb; b++) {
+        norms[b] = std::sqrt(norms[b]);
+        if (!std::isfinite(norms[b])) bad = true;
+    }
+    if (bad) return fail(SPARC_ERR_NONFINITE, "sparc_check_state: non-finite v_z (the solve diverged)");
     return SPARC_OK;
 }
 

@@ -375,6 +375,14 @@ class WaveSolver:
 
     LAUNCHES_PER_STEP = 12  # 6 row passes, 5 column passes, 1 end-of-step pass
 
+    def check(self) -> np.ndarray:
+        """L2 norm of v_z per solve (rms_hist, driver.f90:364-383); raises SparcError with code
+        'non-finite state' if any solve diverged."""
+        out = np.zeros(self.nb)
+        capi.check(self.L.sparc_check_state(self.plan, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                            _stream()), "sparc_check_state")
+        return out
+
     def time(self) -> int:
         t = ctypes.c_int()
         capi.check(self.L.sparc_get_time(self.plan, ctypes.byref(t), _stream()), "sparc_get_time")

@@ -161,3 +161,25 @@ def test_fp32_tracks_fp64():
     s32 = w32.forward().cpu().numpy()
     w32.close()
     assert rel_l2(s32, s64) < FP32_TOL
+
+
+def test_state_check_detects_divergence():
+    """Failure detection on the host side of the ABI: a non-finite state (planted through
+    sparc_set_state, no device fault) is reported as SPARC_ERR_NONFINITE; a healthy state's norm
+    equals the L2 norm of v_z (rms_hist)."""
+    import torch
+    from sparc_flows_gb300.capi import SparcError
+    run, model, psi, cmul = make_case(nsteps=30)
+    ws = gpu_solver(run, model, psi, cmul, nb=2)
+    ws.set_forward_sources([M.SourceSpec(0.0), M.SourceSpec(20.0)])
+    ws.forward()
+    st = ws.state()
+    norms = ws.check()
+    ref = torch.linalg.vector_norm(st[:, 3].reshape(2, -1), dim=1).cpu().numpy()
+    assert np.allclose(norms, ref, rtol=1e-12)
+    bad = st.clone()
+    bad[1, 3, 100, 7] = float("nan")
+    ws.set_state(bad)
+    with pytest.raises(SparcError, match="non-finite"):
+        ws.check()
+    ws.close()
