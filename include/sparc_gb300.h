@@ -148,6 +148,19 @@ int sparc_kernels(sparc_plan_t *plan, const void *fsn, int nfwd, const void *asn
  * dumps and their re-reading (all_modules.f90:750-784, kernels.f90:258-280). */
 int sparc_kernels_accumulate(sparc_plan_t *plan, const void *fsn, int nfwd, int jf, double *out, void *stream);
 
+/* sparc_kernels_accumulate without any device allocation.  No counterpart in the reference:
+ * it serves callers that must not see the library allocate device memory during a run (a
+ * caller capturing the adjoint loop in a CUDA graph, or one whose allocator owns all device
+ * memory).  Its scratch (the x-derivatives of one record pair, nbatch*4*nz*nx values of the
+ * plan precision) is a file-scope device array of 8 MiB held by every GPU that loads the
+ * library until exit; larger batches return SPARC_ERR_SIZE.  The first call on a device looks
+ * up the array's address (cudaGetSymbolAddress) and should come before any stream capture.
+ * Every call reuses the same array: calls that overlap on the GPU (other streams, other
+ * plans) race and must be serialised by the caller.  Nothing in the array needs clearing: each
+ * call writes every element it reads.  Same arguments and results as sparc_kernels_accumulate. */
+int sparc_kernels_accumulate_static(sparc_plan_t *plan, const void *fsn, int nfwd, int jf, double *out,
+                                    void *stream);
+
 /* Host-only FP64 evaluation of the partitioned compact-derivative algebra that the device
  * code applies (no GPU needed): x[nz][n1] = dbyd2(b, ibc) without the stretch factor, with
  * the same chunking as a plan whose chunks hold at most lmax rows.  For validating the

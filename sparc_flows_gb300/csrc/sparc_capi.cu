@@ -15,6 +15,11 @@
 
 using namespace sparc;
 
+namespace sparc {
+template <typename T>
+int kernels_accumulate_static_impl(const KAccArgs<T> &proto, cudaStream_t st, std::string &err);
+}
+
 namespace {
 
 thread_local std::string g_err;
@@ -814,6 +819,30 @@ int sparc_get_time(sparc_plan_t *p, int *time, void *stream)
 
 namespace {
 template <typename T>
+KAccArgs<T> kacc_args(sparc_plan *p, const void *fsn, int nfwd, const void *adj, long long adj_stride, int jf,
+                      double *out)
+{
+    Solver<T> &S = solver<T>(p);
+    const sparc_config_t &c = p->cfg;
+    const size_t F = S.F;
+    KAccArgs<T> k{};
+    k.nx = c.nx; k.nz = c.nz; k.nb = c.nbatch;
+    k.fsn = (const T *)fsn;
+    k.fbase = (long long)jf * 6 * F;
+    k.fstride = (long long)nfwd * 6 * F;
+    k.adj = (const T *)adj;
+    k.astride = adj_stride;
+    k.out = out;
+    k.work = nullptr;
+    k.stretch = S.a.stretch;
+    k.twr = S.fft.twr; k.twi = S.fft.twi; k.kap = S.fft.kap;
+    k.stretchx = (T)c.stretchx;
+    k.z1 = S.z[1].tab;
+    k.nch = p->nch; k.L = p->L;
+    return k;
+}
+
+template <typename T>
 int kernels_impl(sparc_plan *p, const void *fsn, int nfwd, const void *adj, long long adj_stride, int jf, double *out,
                  cudaStream_t st)
 {
@@ -875,6 +904,24 @@ int sparc_kernels_accumulate(sparc_plan_t *p, const void *fsn, int nfwd, int jf,
     if (p->cfg.precision == 32)
         return kernels_impl<float>(p, fsn, nfwd, p->s32.a.A + 2 * F, (long long)4 * F, jf, out, (cudaStream_t)stream);
     return kernels_impl<double>(p, fsn, nfwd, p->s64.a.A + 2 * F, (long long)4 * F, jf, out, (cudaStream_t)stream);
+}
+
+int sparc_kernels_accumulate_static(sparc_plan_t *p, const void *fsn, int nfwd, int jf, double *out, void *stream)
+{
+    if (!p || !fsn || !out || nfwd < 1 || jf < 0 || jf >= nfwd)
+        return fail(SPARC_ERR_ARG, "sparc_kernels_accumulate_static: bad argument");
+    if (!p->have_bg) return fail(SPARC_ERR_STATE, "sparc_kernels_accumulate_static: background must be set first");
+    const size_t F = (size_t)p->cfg.nx * p->cfg.nz;
+    std::string err;
+    int rc;
+    if (p->cfg.precision == 32)
+        rc = kernels_accumulate_static_impl<float>(kacc_args<float>(p, fsn, nfwd, p->s32.a.A + 2 * F, (long long)4 * F, jf, out),
+                                                   (cudaStream_t)stream, err);
+    else
+        rc = kernels_accumulate_static_impl<double>(kacc_args<double>(p, fsn, nfwd, p->s64.a.A + 2 * F, (long long)4 * F, jf, out),
+                                                    (cudaStream_t)stream, err);
+    if (rc != SPARC_OK) return fail(rc, err);
+    return SPARC_OK;
 }
 
 // Host evaluation of the partitioned compact-derivative tables (FP64), the same algebra the
