@@ -80,7 +80,7 @@ bool chunking(int nz, int lmax, int &nch, int &L)
 {
     nch = (nz + lmax - 1) / lmax;
     L = (nz + nch - 1) / nch;
-    if (nch > (lmax >= 32 ? 12 : 20)) return false;  // block geometry of sparc_col.cu
+    if (nch > 20) return false;  // block geometry of sparc_col.cu (ColCfg MAXNCH)
     return nz - (nch - 1) * L >= 2 && L >= 2;
 }
 
@@ -395,6 +395,15 @@ int alloc_solver(sparc_plan *p)
     a.bgz = c.bg_per_solve ? (long long)nzpml * nx : 0;
     a.bgx = c.bg_per_solve ? (long long)nz * nhx : 0;
     a.dt = (T)c.deltat; a.stretchx = (T)c.stretchx; a.fsign = T(1);
+    a.ALO = nullptr;
+    if (sizeof(T) == 4) {  // low parts of the FP32 state (compensated update)
+        void *ptr = nullptr;
+        cudaError_t e = cudaMalloc(&ptr, (size_t)nb * 4 * F * sizeof(T));
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        S.allocs.push_back(ptr);
+        cudaMemset(ptr, 0, (size_t)nb * 4 * F * sizeof(T));
+        a.ALO = (T *)ptr;
+    }
     a.A = A; a.SV = SV; a.P = P; a.RVXP = RVXP; a.DX = DX; a.FXX = FXX; a.FXZ = FXZ; a.TOPDX = TOPDX;
     a.PZ = PZ; a.SPZ = SPZ; a.PX = PX; a.SPX = SPX;
     a.rhoinv = rhoinv; a.rho0 = rho0; a.gp0 = gp0; a.gr0 = gr0; a.g = g; a.stretch = stretch;
@@ -605,6 +614,7 @@ int reset_state(sparc_plan *p, int time0, cudaStream_t st)
     const size_t F = S.F;
     const int nb = c.nbatch, nzpml = c.npmlbot + c.npmltop, nhx = 2 * c.npmlhor;
     CK(cudaMemsetAsync(a.A, 0, (size_t)nb * 4 * F * sizeof(T), st));
+    if (a.ALO) CK(cudaMemsetAsync(a.ALO, 0, (size_t)nb * 4 * F * sizeof(T), st));
     CK(cudaMemsetAsync(a.SV, 0, (size_t)3 * nb * 2 * F * sizeof(T), st));
     CK(cudaMemsetAsync(a.PZ, 0, (size_t)nb * 2 * nzpml * c.nx * sizeof(T), st));
     CK(cudaMemsetAsync(a.SPZ, 0, (size_t)3 * nb * 2 * nzpml * c.nx * sizeof(T), st));
@@ -648,7 +658,7 @@ int sparc_plan_create(const sparc_config_t *cfg, sparc_plan_t **out)
     if (!check_cfg(cfg, why)) return fail(SPARC_ERR_SIZE, "sparc_plan_create: " + why);
     sparc_plan *p = new sparc_plan();
     p->cfg = *cfg;
-    const int lmax = cfg->precision == 32 ? 32 : 16;
+    const int lmax = 16;  // rows per z-chunk (sparc_col.cu ColCfg)
     if (!chunking(cfg->nz, lmax, p->nch, p->L) || !chunking(cfg->nz, 16, p->nch64, p->L64)) {
         delete p;
         return fail(SPARC_ERR_SIZE, "sparc_plan_create: nz too large for the column chunking");
@@ -776,8 +786,9 @@ int sparc_set_state(sparc_plan_t *p, const void *src, void *stream)
     if (!p || !src) return fail(SPARC_ERR_ARG, "sparc_set_state: bad argument");
     const size_t es = p->cfg.precision == 32 ? 4 : 8;
     void *dst = p->cfg.precision == 32 ? (void *)p->s32.a.A : (void *)p->s64.a.A;
-    CK(cudaMemcpyAsync(dst, src, (size_t)p->cfg.nbatch * 4 * p->cfg.nx * p->cfg.nz * es, cudaMemcpyDeviceToDevice,
-                       (cudaStream_t)stream));
+    const size_t bytes = (size_t)p->cfg.nbatch * 4 * p->cfg.nx * p->cfg.nz * es;
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    if (p->cfg.precision == 32 && p->s32.a.ALO) CK(cudaMemsetAsync(p->s32.a.ALO, 0, bytes, (cudaStream_t)stream));
     return SPARC_OK;
 }
 

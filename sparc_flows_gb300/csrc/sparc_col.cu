@@ -21,7 +21,7 @@ template <typename T>
 struct ColCfg;
 template <>
 struct ColCfg<float> {
-    static constexpr int CW = 32, LMAX = 32, MAXNCH = 12;
+    static constexpr int CW = 32, LMAX = 16, MAXNCH = 20;
 };
 template <>
 struct ColCfg<double> {
@@ -69,10 +69,10 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepAr
         if (m < n) {
             const int k = k0 + m;
             const size_t q = (size_t)k * nx + x;
-            T v = Ab[F_XIZ * F + q];
+            T v = __ldg(Ab + F_XIZ * F + q);
             if (s >= 2) {
-                T avz = Ab[F_VZ * F + q];
-                T t = (s == 2) ? avz : avz + bsm1 * svp(a, a.slot_sm2, b, 1)[q];
+                T avz = __ldg(Ab + F_VZ * F + q);
+                T t = (s == 2) ? avz : avz + bsm1 * __ldg(svp(a, a.slot_sm2, b, 1) + q);
                 if (k == 0 || x == 0 || x == nx - 1) t = T(0);
                 v += bs * t;
             }
@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepAr
     __syncthreads();
     // ---- B: local solve of d xi_z/dz
     T y[LMAX];
-    const T preset3 = -a.TOPDX[(size_t)b * nx + x] * a.unstretch_top;
+    const T preset3 = -__ldg(a.TOPDX + (size_t)b * nx + x) * a.unstretch_top;
     const T ylast_yb0 = zlocal<T, LMAX>(a.z3, B0, CW, c, k0, n, nz, preset3, y);
     yb0[(2 * j) * CW + c] = y[0];
     yb0[(2 * j + 1) * CW + c] = ylast_yb0;
@@ -103,13 +103,13 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepAr
                 if (pi >= 0) {
                     const size_t qz = ((size_t)b * 2 * a.nzpml + pi) * nx + x;  // psi_vz
                     const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
-                    T ps = a.PZ[qz];
-                    if (s >= 2) ps += bs * a.SPZ[(size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz];
+                    T ps = __ldg(a.PZ + qz);
+                    if (s >= 2) ps += bs * __ldg(a.SPZ + (size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz);
                     a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz] = __ldg(a.az + qb) * dzz + __ldg(a.bz + qb) * ps;
                     dzz += ps;
                     fd = __ldg(a.fdz + qb);
                 }
-                const T div = a.DX[(size_t)b * F + q] + dzz;
+                const T div = __ldg(a.DX + (size_t)b * F + q) + dzz;
                 const T c2r = a.c2d ? __ldg(a.c2rho0 + (size_t)b * a.bg2 + q) : __ldg(a.c2rho0 + k);
                 const T gp = __ldg(a.gp0 + k) * fd, gr = __ldg(a.gr0 + k) * fd;
                 const T p = -c2r * div - gp * xz[m];
@@ -117,8 +117,8 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepAr
                 xz[m] = rho * __ldg(a.g + k);
                 B1[k * CW + c] = p;
                 a.P[(size_t)b * F + q] = p;
-                T vx = Ab[F_VX * F + q];
-                if (s >= 2) vx += bs * svp(a, a.slot_sm1, b, 0)[q];
+                T vx = __ldg(Ab + F_VX * F + q);
+                if (s >= 2) vx += bs * __ldg(svp(a, a.slot_sm1, b, 0) + q);
                 B0[k * CW + c] = vx;
             }
         }
@@ -151,8 +151,8 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepAr
                 if (pi >= 0) {
                     const size_t qz = (((size_t)b * 2 + 1) * a.nzpml + pi) * nx + x;  // psi_p
                     const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
-                    T ps = a.PZ[qz];
-                    if (s >= 2) ps += bs * a.SPZ[(size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz];
+                    T ps = __ldg(a.PZ + qz);
+                    if (s >= 2) ps += bs * __ldg(a.SPZ + (size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz);
                     a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz] = __ldg(a.az + qb) * gpz + __ldg(a.bz + qb) * ps;
                     gpz += ps;
                 }
@@ -160,11 +160,11 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepAr
                 T rv = T(0);
                 if (a.flows) {
                     const T dvxdz = zcorrect(a.z1, y2[m], k, xl2, xr2) * __ldg(a.stretch + k);
-                    rv = a.FXX[(size_t)b * F + q] - T(2) * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvxdz;
+                    rv = __ldg(a.FXX + (size_t)b * F + q) - T(2) * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvxdz;
                 }
                 a.RVXP[(size_t)b * F + q] = rv;
-                T vz = Ab[F_VZ * F + q];
-                if (s >= 2) vz += bs * svp(a, a.slot_sm1, b, 1)[q];
+                T vz = __ldg(Ab + F_VZ * F + q);
+                if (s >= 2) vz += bs * __ldg(svp(a, a.slot_sm1, b, 1) + q);
                 B1[k * CW + c] = vz;
             }
         }
@@ -189,9 +189,9 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepAr
         for (int jj = 0; jj < 7; jj++) {
             const int r = i0 + jj;
             if (r >= 0 && r < a.nrows && w[jj] != 0.0)
-                f += w[jj] * (double)a.src_rows[((size_t)b * a.nrows + r) * nx + x];
+                f += w[jj] * (double)__ldg(a.src_rows + ((size_t)b * a.nrows + r) * nx + x);
         }
-        forcing = T(f) * a.inj_scale[(size_t)b * nx + x];
+        forcing = T(f) * __ldg(a.inj_scale + (size_t)b * nx + x);
     }
     T *svz = svp(a, a.slot_s, b, 1);
 #pragma unroll
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepAr
             if (k == a.k_inj) r += forcing;
             if (a.flows) {
                 const T dvzdz = zcorrect(a.z1, y2[m], k, xl2, xr2) * __ldg(a.stretch + k);
-                r += a.FXZ[(size_t)b * F + q] - T(2) * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvzdz;
+                r += __ldg(a.FXZ + (size_t)b * F + q) - T(2) * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvzdz;
             }
             if (k == 0 || x == 0 || x == nx - 1) r = T(0);
             svz[q] = r;
@@ -220,6 +220,108 @@ __device__ __forceinline__ T filt11(const T *B, int CW, int c, int k)
     return c0 * B[k * CW + c] + h1 * (B[(k - 1) * CW + c] + B[(k + 1) * CW + c]) +
            h2 * (B[(k - 2) * CW + c] + B[(k + 2) * CW + c]) + h3 * (B[(k - 3) * CW + c] + B[(k + 3) * CW + c]) +
            h4 * (B[(k - 4) * CW + c] + B[(k + 4) * CW + c]) + h5 * (B[(k - 5) * CW + c] + B[(k + 5) * CW + c]);
+}
+
+// Double-float helpers (Knuth TwoSum, FMA-based exact product) for the FP32 state update.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void df_add(float &hi, float &lo, float bh, float bl)
+{
+    float s, e;
+    two_sum(hi, bh, s, e);
+    e += lo + bl;
+    hi = s + e;
+    lo = e - (hi - s);
+}
+
+// h * (x + y) for double-float x, y and an exact binary coefficient h, added to (hi, lo).
+__device__ __forceinline__ void df_axpy2(float &hi, float &lo, float h, float xh, float xl, float yh, float yl)
+{
+    float s, e;
+    two_sum(xh, yh, s, e);
+    e += xl + yl;
+    const float p = h * s;
+    const float pe = fmaf(h, s, -p) + h * e;
+    df_add(hi, lo, p, pe);
+}
+
+// End of step for FP32 plans carrying low parts: a + deltat scr and FILTER_VARS_2D evaluated in
+// double-float arithmetic, so the state keeps ~48 bits across the 3600 steps instead of
+// accumulating one FP32 rounding of |a| per step.
+__device__ __forceinline__ float filt11_df(const float *H, const float *Lo, int CW, int c, int k, float &lo)
+{
+    float hi = 0.f;
+    lo = 0.f;
+    const float c0 = 0.75390625f, h1 = 0.205078125f, h2 = -0.1171875f, h3 = 0.0439453125f, h4 = -0.009765625f,
+                h5 = 0.0009765625f;
+    {
+        const float p = c0 * H[k * CW + c];
+        const float pe = fmaf(c0, H[k * CW + c], -p) + c0 * Lo[k * CW + c];
+        df_add(hi, lo, p, pe);
+    }
+    const float hs[5] = {h1, h2, h3, h4, h5};
+#pragma unroll
+    for (int j = 1; j <= 5; j++)
+        df_axpy2(hi, lo, hs[j - 1], H[(k - j) * CW + c], Lo[(k - j) * CW + c], H[(k + j) * CW + c],
+                 Lo[(k + j) * CW + c]);
+    return hi;
+}
+
+template <int CW>
+__device__ void end_step_compensated(const StepArgs<float> &a, float *B0, float *B1, int c, int x, int b, int k0, int n,
+                                     bool record, int rec, float *snap)
+{
+    const int nz = a.nz, nx = a.nx;
+    const size_t F = (size_t)nz * nx;
+    float *Ab = a.A + (size_t)b * 4 * F;
+    float *Lb = a.ALO + (size_t)b * 4 * F;
+    const bool xf = (x >= a.nh - 1) && (x <= nx - a.nh);
+    for (int f = 0; f < 4; f++) {
+        for (int m = 0; m < n; m++) {
+            const int k = k0 + m;
+            const size_t q = (size_t)k * nx + x;
+            float sc;
+            if (f == F_XIX || f == F_XIZ) {
+                const int cc = (f == F_XIX) ? 0 : 1;
+                sc = Ab[(f == F_XIX ? F_VX : F_VZ) * F + q] + a.bs * svp(a, a.slot_sm1, b, cc)[q];
+                if (k == 0 || x == 0 || x == nx - 1) sc = 0.f;
+            } else {
+                sc = svp(a, a.slot_s, b, f == F_VX ? 0 : 1)[q];
+            }
+            float hi = Ab[f * F + q], lo = Lb[f * F + q];
+            const float d = a.dt * sc;
+            df_add(hi, lo, d, fmaf(a.dt, sc, -d));
+            B0[k * CW + c] = hi;
+            B1[k * CW + c] = lo;
+        }
+        __syncthreads();
+        for (int m = 0; m < n; m++) {
+            const int k = k0 + m;
+            const size_t q = (size_t)k * nx + x;
+            float hi = B0[k * CW + c], lo = B1[k * CW + c];
+            if (xf && k >= 5 && k <= nz - 2) {
+                if (k <= nz - 6) {
+                    hi = filt11_df(B0, B1, CW, c, k, lo);
+                } else {
+                    float h = 0.f, l = 0.f;
+                    df_axpy2(h, l, 0.5f, B0[(k + 1) * CW + c], B1[(k + 1) * CW + c], B0[(k - 1) * CW + c],
+                             B1[(k - 1) * CW + c]);
+                    hi = h;
+                    lo = l;
+                }
+            }
+            Ab[f * F + q] = hi;
+            Lb[f * F + q] = lo;
+            if (snap) snap[(size_t)f * F + q] = hi;
+            if (record && f == F_VZ && k == a.k_obs && a.seis) a.seis[((size_t)b * a.nrec_cap + rec) * nx + x] = hi;
+        }
+        __syncthreads();
+    }
 }
 
 template <typename T, int CW, int LMAX>
@@ -240,6 +342,12 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) end_step_kernel(StepArg
     const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec < a.nrec_cap && time >= 0;
     const bool xf = (x >= a.nh - 1) && (x <= nx - a.nh);
     T *snap = record && a.snaps ? a.snaps + ((size_t)b * a.nrec_cap + rec) * 6 * F : nullptr;
+    if constexpr (sizeof(T) == 4) {
+        if (a.ALO) {
+            end_step_compensated<CW>(a, B0, B0 + (size_t)nz * CW, c, x, b, k0, n, record, rec, snap);
+            goto aux;
+        }
+    }
     for (int f = 0; f < 4; f++) {
         for (int m = 0; m < n; m++) {
             {
@@ -274,6 +382,7 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) end_step_kernel(StepArg
         }
         __syncthreads();
     }
+aux:
     for (int m = 0; m < n; m++) {
         {
             const int k = k0 + m;
@@ -377,7 +486,7 @@ cudaError_t launch_end_step(const StepArgs<T> &a, cudaStream_t st)
 {
     constexpr int CW = ColCfg<T>::CW, LMAX = ColCfg<T>::LMAX;
     if (a.nx % CW || a.L > LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
-    const size_t smem = (size_t)a.nz * CW * sizeof(T);
+    const size_t smem = (size_t)a.nz * CW * sizeof(T) * (a.ALO ? 2 : 1);
     auto k = end_step_kernel<T, CW, LMAX>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid(a.nx / CW, a.nb);

@@ -35,7 +35,7 @@ struct ZTab {
 };
 
 // Everything one stage kernel needs.  Layouts (x fastest everywhere):
-//   A    [nb][4][nz][nx]            state xi_x, xi_z, v_x, v_z
+//   A    [nb][4][nz][nx]            state xi_x, xi_z, v_x, v_z (ALO: low parts, FP32 plans)
 //   SV   [3][nb][2][nz][nx]         ring of stage RHS of v_x, v_z (slot = stage % 3)
 //   P, RVXP, DX, FXX, FXZ [nb][nz][nx] stage intermediates, TOPDX [nb][nx]
 //   PZ   [nb][2][nzpml][nx]         psi_vz, psi_p;  SPZ [3][nb][2][nzpml][nx]
@@ -48,6 +48,7 @@ struct StepArgs {
     T bs, bsm1, dt, stretchx, fsign, unstretch_top;
     int stage, slot_s, slot_sm1, slot_sm2;
     T *A, *SV, *P, *RVXP, *DX, *FXX, *FXZ, *TOPDX, *PZ, *SPZ, *PX, *SPX;
+    T *ALO;  // low parts of the state (FP32 plans): A + ALO carries ~48 significant bits
     const T *rhoinv, *rho0, *gp0, *gr0, *g, *stretch;
     const T *fdz, *az, *bz, *ax, *bx, *c2rho0, *v0x, *v0z;
     const T *twr, *twi, *kap;

@@ -45,14 +45,14 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
     // ---- load: (p_{s-1}, xi_x at stage s) or (p_5, 0)
     for (int x = lane; x < nx; x += WARP) {
         T p = T(0), xis = T(0);
-        if (MODE != 0) p = a.P[(size_t)b * F + ro + x];
+        if (MODE != 0) p = __ldg(a.P + (size_t)b * F + ro + x);
         if (MODE == 0) {
-            xis = Ab[F_XIX * F + ro + x];
+            xis = __ldg(Ab + F_XIX * F + ro + x);
         } else if (MODE == 1) {
-            T avx = Ab[F_VX * F + ro + x];
-            T s = (a.stage == 2) ? avx : avx + bsm1 * svp(a, a.slot_sm2, b, 0)[ro + x];
+            T avx = __ldg(Ab + F_VX * F + ro + x);
+            T s = (a.stage == 2) ? avx : avx + bsm1 * __ldg(svp(a, a.slot_sm2, b, 0) + ro + x);
             if (k == 0 || x == 0 || x == nx - 1) s = T(0);  // RHS boundary zeros (physics2d.f90:1083-1093)
-            xis = Ab[F_XIX * F + ro + x] + bs * s;
+            xis = __ldg(Ab + F_XIX * F + ro + x) + bs * s;
         }
         xr[x] = p;
         xi[x] = xis;
@@ -86,16 +86,16 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
         }
         T svx = T(0);
         if (MODE != 0) {
-            svx = a.RVXP[(size_t)b * F + ro + x] - rhoinv_k * gpx;
+            svx = __ldg(a.RVXP + (size_t)b * F + ro + x) - rhoinv_k * gpx;
             if (k == 0 || x == 0 || x == nx - 1) svx = T(0);
             svp(a, a.slot_sm1, b, 0)[ro + x] = svx;
         }
         if (MODE != 2) {
             a.DX[(size_t)b * F + ro + x] = dxx;
-            T vxs = Ab[F_VX * F + ro + x], vzs = Ab[F_VZ * F + ro + x];
+            T vxs = __ldg(Ab + F_VX * F + ro + x), vzs = __ldg(Ab + F_VZ * F + ro + x);
             if (MODE == 1) {
                 vxs += bs * svx;
-                vzs += bs * svp(a, a.slot_sm1, b, 1)[ro + x];
+                vzs += bs * __ldg(svp(a, a.slot_sm1, b, 1) + ro + x);
             }
             o1r[x] = vxs;
             o1i[x] = vzs;
