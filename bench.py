@@ -208,6 +208,26 @@ def run_gpu(args):
     # ---- per-pass timing (CUDA events on the launching stream, outside the timed loop)
     passes = pipe.fwd.profile_passes(nsteps=20)
 
+    # ---- the FP64 plain single-source path (plain64: nx=256, no flow, 1800 steps), same pipeline
+    plain = None
+    if not args.no_plain:
+        prun, pmodel, pspecs, ppsi, pcmul = M.workload("plain64")
+        if args.nsteps:
+            prun = prun.replace(nsteps=min(args.nsteps, prun.nsteps))
+        pp = FwdAdjKernels(prun, pmodel, pspecs, psi=ppsi, cmul=pcmul, precision=64, device=dev)
+        pp.run_all()
+        torch.cuda.synchronize()
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        for _ in range(2):
+            pp.run_all()
+        q1.record(stream)
+        torch.cuda.synchronize()
+        pms = q0.elapsed_time(q1) / 2
+        plain = {"workload": "plain64: 1 source, nx=256 (200 Mm), nz=300, no flow, 1800 steps, FP64",
+                 "value": pp.point_steps() / (pms * 1e-3), "unit": UNIT, "ms_per_run": pms}
+        pp.close()
+
     # ---- end-to-end through the public API: pinned host inputs in, host kernels/seismograms out
     nrec = run.nrec
     data_h = torch.zeros((len(specs), nrec, run.nx), dtype=torch.float32).pin_memory()
@@ -262,6 +282,9 @@ def run_gpu(args):
                     "steps": e2e_steps},
             "gpu_launches": pipe.launch_count() * args.steps,
         }
+        if plain is not None:
+            plain["fp32_batched_over_fp64_plain"] = (value / world) / plain["value"]
+            line["fp64_plain"] = plain
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_quick()
         print(json.dumps(line), flush=True)
@@ -278,6 +301,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nsteps", type=int, default=0, help="override the 3600 time steps (testing only)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain reference path")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -47,6 +47,11 @@ typedef struct {
     int k_inj;                 /* 0-based injection row (e_rad forward, o_rad adjoint) */
     int k_obs;                 /* 0-based observation row o_rad (physics2d.f90:43-50) */
     int src_until;             /* inject while time <= src_until (physics2d.f90:1049) */
+    int filter_k0;             /* first 0-based row FILTER_VARS_2D writes: 5 as the reference
+                                  (kst = 6), 1 to also apply its 2-point rows 2..5 (the
+                                  commented-out kst = 2, physics2d.f90:545) */
+    int filter_all_x;          /* 0: filter only x in [npmlhor, nx-npmlhor+1] (HORIZONTAL_PMLS,
+                                  physics2d.f90:548-556); 1: every column */
 } sparc_config_t;
 
 /* Background, all DEVICE pointers to FP64 arrays; copied (and rounded for FP32 plans) into

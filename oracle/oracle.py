@@ -29,6 +29,7 @@ class OrcParams(ctypes.Structure):
         ("excitdep", ctypes.c_double), ("obsheight", ctypes.c_double),
         ("flows", ctypes.c_int), ("adjoint", ctypes.c_int), ("steps_out", ctypes.c_int),
         ("src_until", ctypes.c_int), ("cadforcing", ctypes.c_double),
+        ("filter_kst", ctypes.c_int), ("filter_all_x", ctypes.c_int),
     ]
 
 
@@ -86,7 +87,8 @@ def params_from(run):
     """Build OrcParams from a sparc_flows_gb300.config.RunConfig-like object."""
     return OrcParams(run.nx, run.nz, run.npmlbot, run.npmltop, run.npmlhor, run.xlength_cm,
                      run.timestep, run.excitdep_cm, run.obsheight_cm, int(run.flows),
-                     int(run.adjoint), run.steps_out, run.src_until, run.cadforcing)
+                     int(run.adjoint), run.steps_out, run.src_until, run.cadforcing,
+                     getattr(run, "filter_kst", 6), int(getattr(run, "filter_all_x", False)))
 
 
 class OracleSim:

@@ -253,6 +253,8 @@ typedef struct {
     int steps_out;    /* steps = floor(outputcad/timestep), driver.f90:209 */
     int src_until;    /* forcing_length*cadforcing_step, physics2d.f90:1049 */
     double cadforcing;/* params.i:46 */
+    int filter_kst;   /* first row (1-based) FILTER_VARS_2D writes: 6 as physics2d.f90:544 */
+    int filter_all_x; /* 1: filter every column instead of [npmlhor, nx-npmlhor+1] */
 } orc_params;
 
 typedef struct orc_sim {
@@ -744,8 +746,16 @@ static void orc_filter_vars_2d(orc_sim *s)
             T_(nz - 3, i) = 0.5 * (A_(nz - 2, i) + A_(nz - 4, i));
             T_(nz - 2, i) = 0.5 * (A_(nz - 1, i) + A_(nz - 3, i));
         }
-        for (int k = 5; k <= nz - 2; k++) /* kst = 6 .. nz-1 (1-based) */
-            for (int i = nh - 1; i <= nx - nh; i++) A_(k, i) = T_(k, i);
+        for (int i = 0; i < nx; i++) { /* temp(2..5) under USE_PML, physics2d.f90:539-544 */
+            T_(1, i) = 0.5 * (A_(2, i) + A_(0, i));
+            T_(2, i) = 0.5 * (A_(3, i) + A_(1, i));
+            T_(3, i) = 0.5 * (A_(4, i) + A_(2, i));
+            T_(4, i) = 0.5 * (A_(5, i) + A_(3, i));
+        }
+        int kst = s->p.filter_kst > 0 ? s->p.filter_kst : 6;
+        int i0 = s->p.filter_all_x ? 0 : nh - 1, i1 = s->p.filter_all_x ? nx - 1 : nx - nh;
+        for (int k = kst - 1; k <= nz - 2; k++) /* kst .. nz-1 (1-based) */
+            for (int i = i0; i <= i1; i++) A_(k, i) = T_(k, i);
 #undef A_
 #undef T_
     }

@@ -35,6 +35,8 @@ class RunConfig:
     cadforcing: float = 30.0         # params.i:46 (s)
     nsteps: int = 3600               # number of time steps to run
     solartime_h: float = 4.0         # params.i:132
+    filter_kst: int = 6              # first row (1-based) FILTER_VARS_2D writes (physics2d.f90:544-545)
+    filter_all_x: bool = False       # filter the horizontal-PML columns too (physics2d.f90:548-556)
 
     @property
     def steps_out(self) -> int:

@@ -413,6 +413,7 @@ int alloc_solver(sparc_plan *p)
     a.nch = p->nch; a.L = p->L;
     a.d_time = p->d_time;
     a.src_until = c.src_until; a.k_inj = c.k_inj; a.k_obs = c.k_obs; a.steps_out = c.steps_out;
+    a.filt_k0 = c.filter_k0; a.filt_xall = c.filter_all_x;
     a.inj_scale = inj; a.src_rows = rows; a.nrows = 1;
     return SPARC_OK;
 }
@@ -631,13 +632,13 @@ bool check_cfg(const sparc_config_t *c, std::string &why)
     if (c->precision != 32 && c->precision != 64) { why = "precision must be 32 or 64"; return false; }
     if (c->nbatch < 1) { why = "nbatch < 1"; return false; }
     if (!fft_size_supported(c->nx)) { why = "nx not supported by the FFT (64..1024, 2^a 3^b)"; return false; }
-    const int cw = c->precision == 32 ? 32 : 16;
-    if (c->nx % cw) { why = "nx must be a multiple of the column width"; return false; }
+    if (c->nx % 8) { why = "nx must be a multiple of 8 (column block width)"; return false; }
     if (c->nz < 16) { why = "nz < 16"; return false; }
     if (c->npmlbot < 1 || c->npmltop < 1 || c->npmlbot + c->npmltop >= c->nz) { why = "bad vertical PML size"; return false; }
     if (c->npmlhor < 1 || 2 * c->npmlhor >= c->nx) { why = "bad horizontal PML size"; return false; }
     if (c->k_inj < 1 || c->k_inj > c->nz - 2 || c->k_obs < 0 || c->k_obs >= c->nz) { why = "bad injection/observation row"; return false; }
     if (c->steps_out < 1) { why = "steps_out < 1"; return false; }
+    if (c->filter_k0 < 1 || c->filter_k0 > 5) { why = "filter_k0 must be 1..5 (5: the reference)"; return false; }
     return true;
 }
 

@@ -19,13 +19,15 @@ namespace sparc {
 // Column-block geometry: CW columns per block, at most MAXNCH chunks of at most LMAX rows.
 template <typename T>
 struct ColCfg;
+// Narrow blocks (8 columns = one 32-byte sector per row for FP32) so that several blocks are
+// resident per SM and their barrier-separated phases overlap each other's memory latency.
 template <>
 struct ColCfg<float> {
-    static constexpr int CW = 32, LMAX = 16, MAXNCH = 20;
+    static constexpr int CW = 8, LMAX = 16, MAXNCH = 20, MINB = 4;
 };
 template <>
 struct ColCfg<double> {
-    static constexpr int CW = 16, LMAX = 16, MAXNCH = 20;
+    static constexpr int CW = 8, LMAX = 16, MAXNCH = 20, MINB = 2;
 };
 
 template <typename T>
@@ -43,7 +45,7 @@ __device__ __forceinline__ int pml_row(const StepArgs<T> &a, int k)
 }
 
 template <typename T, int CW, int LMAX>
-__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) col_stage_kernel(StepArgs<T> a)
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) col_stage_kernel(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *B0 = reinterpret_cast<T *>(smem_raw);
@@ -280,7 +282,7 @@ __device__ void end_step_compensated(const StepArgs<float> &a, float *B0, float 
     const size_t F = (size_t)nz * nx;
     float *Ab = a.A + (size_t)b * 4 * F;
     float *Lb = a.ALO + (size_t)b * 4 * F;
-    const bool xf = (x >= a.nh - 1) && (x <= nx - a.nh);
+    const bool xf = a.filt_xall || ((x >= a.nh - 1) && (x <= nx - a.nh));
     for (int f = 0; f < 4; f++) {
         for (int m = 0; m < n; m++) {
             const int k = k0 + m;
@@ -304,8 +306,8 @@ __device__ void end_step_compensated(const StepArgs<float> &a, float *B0, float 
             const int k = k0 + m;
             const size_t q = (size_t)k * nx + x;
             float hi = B0[k * CW + c], lo = B1[k * CW + c];
-            if (xf && k >= 5 && k <= nz - 2) {
-                if (k <= nz - 6) {
+            if (xf && k >= a.filt_k0 && k <= nz - 2) {
+                if (k >= 5 && k <= nz - 6) {
                     hi = filt11_df(B0, B1, CW, c, k, lo);
                 } else {
                     float h = 0.f, l = 0.f;
@@ -325,7 +327,7 @@ __device__ void end_step_compensated(const StepArgs<float> &a, float *B0, float 
 }
 
 template <typename T, int CW, int LMAX>
-__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) end_step_kernel(StepArgs<T> a)
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) end_step_kernel(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *B0 = reinterpret_cast<T *>(smem_raw);
@@ -340,7 +342,7 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) end_step_kernel(StepArg
     const int time = *a.d_time;
     const int rec = (a.steps_out > 0) ? time / a.steps_out : 0;
     const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec < a.nrec_cap && time >= 0;
-    const bool xf = (x >= a.nh - 1) && (x <= nx - a.nh);
+    const bool xf = a.filt_xall || ((x >= a.nh - 1) && (x <= nx - a.nh));
     T *snap = record && a.snaps ? a.snaps + ((size_t)b * a.nrec_cap + rec) * 6 * F : nullptr;
     if constexpr (sizeof(T) == 4) {
         if (a.ALO) {
@@ -370,8 +372,8 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) end_step_kernel(StepArg
                 const int k = k0 + m;
                 const size_t q = (size_t)k * nx + x;
                 T out = B0[k * CW + c];
-                if (xf && k >= 5 && k <= nz - 2) {
-                    if (k <= nz - 6) out = filt11(B0, CW, c, k);
+                if (xf && k >= a.filt_k0 && k <= nz - 2) {
+                    if (k >= 5 && k <= nz - 6) out = filt11(B0, CW, c, k);
                     else out = T(0.5) * (B0[(k + 1) * CW + c] + B0[(k - 1) * CW + c]);
                 }
                 Ab[f * F + q] = out;
@@ -405,7 +407,7 @@ aux:
 // Generic compact derivative of n1 columns: dvar = stretch .* dbyd2(var), optional
 // FILTER_VAR_Z (kernels.f90:891-928) afterwards.
 template <typename T, int CW, int LMAX>
-__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) ddz_kernel(ZTab<T> tb, int nch, int L, const T *__restrict__ var,
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) ddz_kernel(ZTab<T> tb, int nch, int L, const T *__restrict__ var,
                                                          T *__restrict__ dvar, int n1, int nz,
                                                          const T *__restrict__ preset,
                                                          const T *__restrict__ stretch, int filter)
@@ -545,7 +547,7 @@ __device__ __forceinline__ void kacc_dz(const KAccArgs<T> &a, const T *src, T *B
 }
 
 template <typename T, int CW, int LMAX>
-__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH) kacc_col_kernel(KAccArgs<T> a)
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) kacc_col_kernel(KAccArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *B0 = reinterpret_cast<T *>(smem_raw);

@@ -56,6 +56,7 @@ struct StepArgs {
     int nch, L;
     int *d_time;
     int src_until, k_inj, k_obs, steps_out;
+    int filt_k0, filt_xall;  // FILTER_VARS_2D coverage (rows from filt_k0, all columns if filt_xall)
     const T *inj_scale, *src_rows;
     int nrows;
     const double *src_w;

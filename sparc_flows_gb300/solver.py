@@ -122,6 +122,7 @@ class WaveSolver:
             cfg.betas[i] = self.betas[i]
         cfg.flows, cfg.c2d, cfg.bg_per_solve = int(self.flows), int(c2d), int(per_solve)
         cfg.steps_out, cfg.k_inj, cfg.k_obs, cfg.src_until = run.steps_out, k_inj, self.o_rad, run.src_until
+        cfg.filter_k0, cfg.filter_all_x = run.filter_kst - 1, int(run.filter_all_x)
         self.cfg = cfg
         h = ctypes.c_void_p()
         capi.check(self.L.sparc_plan_create(ctypes.byref(cfg), ctypes.byref(h)), "sparc_plan_create")
