@@ -59,6 +59,7 @@ def lib():
                                              ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int]
         L.orc_set_adjoint_source.argtypes = [ctypes.c_void_p, _c_double_p, ctypes.c_int, ctypes.c_int]
         L.orc_step.argtypes = [ctypes.c_void_p]
+        L.orc_apply_filter.argtypes = [ctypes.c_void_p]
         L.orc_run.argtypes = [ctypes.c_void_p, ctypes.c_int, _c_double_p, _c_double_p]
         L.orc_run.restype = ctypes.c_int
         L.orc_get_int.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
@@ -132,6 +133,9 @@ class OracleSim:
 
     def step(self):
         self.L.orc_step(self.h)
+
+    def apply_filter(self):
+        self.L.orc_apply_filter(self.h)
 
     def run_steps(self, nsteps, snapshots=False):
         nrec_max = nsteps // self.run.steps_out + 2

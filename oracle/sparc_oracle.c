@@ -761,6 +761,9 @@ static void orc_filter_vars_2d(orc_sim *s)
     }
 }
 
+/* FILTER_VARS_2D alone on the current state (for the tests). */
+void orc_apply_filter(orc_sim *s) { orc_filter_vars_2d(s); }
+
 /* STEP, step.f90:43-119 */
 void orc_step(orc_sim *s)
 {

@@ -105,9 +105,11 @@ def test_gpu_derivatives_match_oracle(case):
     ws.close()
 
 
-@pytest.mark.parametrize("flows,bump", [(False, False), (True, True)])
-def test_forward_fp64_matches_oracle(flows, bump):
+@pytest.mark.parametrize("flows,bump,kst,allx", [(False, False, 6, False), (True, True, 6, False),
+                                                 (True, True, 2, True)])
+def test_forward_fp64_matches_oracle(flows, bump, kst, allx):
     run, model, psi, cmul = make_case(flows=flows, bump=bump, nsteps=150)
+    run = run.replace(filter_kst=kst, filter_all_x=allx)
     spec = M.SourceSpec(10.0)
     sim = oracle_for(run, model, psi, cmul, spec)
     seis_o = sim.run_steps(run.nsteps)

@@ -115,3 +115,28 @@ def test_forward_run_is_finite_and_linear():
     assert np.all(np.isfinite(outs[0]))
     assert np.abs(outs[0]).max() > 0
     assert np.array_equal(outs[0], outs[1])  # deterministic
+
+
+@pytest.mark.parametrize("kst,allx", [(6, False), (2, False), (2, True)])
+def test_filter_coverage_options(kst, allx):
+    """FILTER_VARS_2D writes rows kst..nz-1 (1-based) of columns [npmlhor, nx-npmlhor+1] (or all
+    columns): 11-point rows 6..nz-5, 2-point averages on rows 2..5 and nz-4..nz-1
+    (physics2d.f90:524-556)."""
+    nz, nx = 60, 64
+    run = RunConfig(nx=nx, nz=nz, xlength_cm=100e8, nsteps=2, flows=False, filter_kst=kst, filter_all_x=allx)
+    sim = O.OracleSim(run, M.polytrope(nz))
+    a6 = np.random.default_rng(kst).standard_normal((6, nz, nx))
+    sim.set_state(a6)
+    sim.apply_filter()
+    out = sim.get("a").reshape(6, nz, nx)
+    sim.close()
+    ref = a6.copy()
+    t = O.np_filter_z(a6[:, :, :].transpose(1, 0, 2))   # (nz, 6, nx)
+    t = t.transpose(1, 0, 2)
+    for k in list(range(1, 5)) + list(range(nz - 5, nz - 1)):
+        t[:, k] = 0.5 * (a6[:, k + 1] + a6[:, k - 1])
+    nh = run.npmlhor
+    cols = slice(0, nx) if allx else slice(nh - 1, nx - nh + 1)
+    rows = slice(kst - 1, nz - 1)
+    ref[:, rows, cols] = t[:, rows, cols]
+    assert np.abs(out - ref).max() <= 1e-14 * np.abs(ref).max()
