@@ -32,7 +32,7 @@ METRIC = "fwd+adj grid-pt-steps/s: FP32 batched vs FP64 plain, 1 GB300, <=1e-4 r
 UNIT = "grid-pt-steps/s"
 
 
-def words_per_point_step(nx, nz, npmlbot=10, npmltop=10, npmlhor=9, V=4, B=3):
+def words_per_point_step(nx, nz, npmlbot=20, npmltop=10, npmlhor=9, V=4, B=3):
     """Algorithmic words per grid-point step of the fused schedule: 15 V + 10 + 5 B + 15 Naux/N."""
     naux = 2 * nx * (npmlbot + npmltop) + 2 * (2 * npmlhor) * nz
     return 15 * V + 10 + 5 * B + 15 * naux / (nx * nz)

@@ -52,6 +52,10 @@ typedef struct {
                                   commented-out kst = 2, physics2d.f90:545) */
     int filter_all_x;          /* 0: filter only x in [npmlhor, nx-npmlhor+1] (HORIZONTAL_PMLS,
                                   physics2d.f90:548-556); 1: every column */
+    int compensated;           /* FP32 plans: 1 keeps a low-order part of the state so the RK
+                                  update and filter round like FP64 arithmetic (no reference
+                                  counterpart; the reference state is FP64) */
+    int column_block;          /* column-pass block width: 32 or 8 x-columns (tuning) */
 } sparc_config_t;
 
 /* Background, all DEVICE pointers to FP64 arrays; copied (and rounded for FP32 plans) into

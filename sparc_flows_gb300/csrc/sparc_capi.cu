@@ -396,7 +396,7 @@ int alloc_solver(sparc_plan *p)
     a.bgx = c.bg_per_solve ? (long long)nz * nhx : 0;
     a.dt = (T)c.deltat; a.stretchx = (T)c.stretchx; a.fsign = T(1);
     a.ALO = nullptr;
-    if (sizeof(T) == 4) {  // low parts of the FP32 state (compensated update)
+    if (sizeof(T) == 4 && c.compensated) {  // low parts of the FP32 state (compensated update)
         void *ptr = nullptr;
         cudaError_t e = cudaMalloc(&ptr, (size_t)nb * 4 * F * sizeof(T));
         if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
@@ -414,6 +414,7 @@ int alloc_solver(sparc_plan *p)
     a.d_time = p->d_time;
     a.src_until = c.src_until; a.k_inj = c.k_inj; a.k_obs = c.k_obs; a.steps_out = c.steps_out;
     a.filt_k0 = c.filter_k0; a.filt_xall = c.filter_all_x;
+    a.colw = (c.column_block == 32 && nx % 32 == 0) ? 32 : 8;
     a.inj_scale = inj; a.src_rows = rows; a.nrows = 1;
     return SPARC_OK;
 }
@@ -851,6 +852,7 @@ KAccArgs<T> kacc_args(sparc_plan *p, const void *fsn, int nfwd, const void *adj,
     k.stretchx = (T)c.stretchx;
     k.z1 = S.z[1].tab;
     k.nch = p->nch; k.L = p->L;
+    k.colw = S.a.colw;
     return k;
 }
 
@@ -881,6 +883,7 @@ int kernels_impl(sparc_plan *p, const void *fsn, int nfwd, const void *adj, long
     k.stretchx = (T)c.stretchx;
     k.z1 = S.z[1].tab;
     k.nch = p->nch; k.L = p->L;
+    k.colw = S.a.colw;
     CK(launch_kacc<T>(k, st));
     return SPARC_OK;
 }

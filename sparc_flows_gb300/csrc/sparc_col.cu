@@ -23,12 +23,14 @@ struct ColCfg;
 // resident per SM and their barrier-separated phases overlap each other's memory latency.
 template <>
 struct ColCfg<float> {
-    static constexpr int CW = 8, LMAX = 16, MAXNCH = 20, MINB = 4;
+    static constexpr int LMAX = 16, MAXNCH = 20;
 };
 template <>
 struct ColCfg<double> {
-    static constexpr int CW = 8, LMAX = 16, MAXNCH = 20, MINB = 2;
+    static constexpr int LMAX = 16, MAXNCH = 20;
 };
+template <typename T, int CW>
+constexpr int min_blocks() { return CW <= 8 ? (sizeof(T) == 4 ? 4 : 2) : 1; }
 
 template <typename T>
 __device__ __forceinline__ T *svp(const StepArgs<T> &a, int slot, int b, int c)
@@ -45,7 +47,7 @@ __device__ __forceinline__ int pml_row(const StepArgs<T> &a, int k)
 }
 
 template <typename T, int CW, int LMAX>
-__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) col_stage_kernel(StepArgs<T> a)
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, (min_blocks<T, CW>())) col_stage_kernel(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *B0 = reinterpret_cast<T *>(smem_raw);
@@ -327,7 +329,7 @@ __device__ void end_step_compensated(const StepArgs<float> &a, float *B0, float 
 }
 
 template <typename T, int CW, int LMAX>
-__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) end_step_kernel(StepArgs<T> a)
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, (min_blocks<T, CW>())) end_step_kernel(StepArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *B0 = reinterpret_cast<T *>(smem_raw);
@@ -407,7 +409,7 @@ aux:
 // Generic compact derivative of n1 columns: dvar = stretch .* dbyd2(var), optional
 // FILTER_VAR_Z (kernels.f90:891-928) afterwards.
 template <typename T, int CW, int LMAX>
-__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) ddz_kernel(ZTab<T> tb, int nch, int L, const T *__restrict__ var,
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, (min_blocks<T, CW>())) ddz_kernel(ZTab<T> tb, int nch, int L, const T *__restrict__ var,
                                                          T *__restrict__ dvar, int n1, int nz,
                                                          const T *__restrict__ preset,
                                                          const T *__restrict__ stretch, int filter)
@@ -464,52 +466,6 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) ddz_ke
 }
 
 
-template <typename T>
-static size_t col_smem(int nz, int nch)
-{
-    return ((size_t)2 * nz * ColCfg<T>::CW + (size_t)8 * nch * ColCfg<T>::CW) * sizeof(T);
-}
-
-template <typename T>
-cudaError_t launch_col_stage(const StepArgs<T> &a, cudaStream_t st)
-{
-    constexpr int CW = ColCfg<T>::CW, LMAX = ColCfg<T>::LMAX;
-    if (a.nx % CW || a.L > LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
-    const size_t smem = col_smem<T>(a.nz, a.nch);
-    auto k = col_stage_kernel<T, CW, LMAX>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid(a.nx / CW, a.nb);
-    k<<<grid, CW * a.nch, smem, st>>>(a);
-    return cudaGetLastError();
-}
-
-template <typename T>
-cudaError_t launch_end_step(const StepArgs<T> &a, cudaStream_t st)
-{
-    constexpr int CW = ColCfg<T>::CW, LMAX = ColCfg<T>::LMAX;
-    if (a.nx % CW || a.L > LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
-    const size_t smem = (size_t)a.nz * CW * sizeof(T) * (a.ALO ? 2 : 1);
-    auto k = end_step_kernel<T, CW, LMAX>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid(a.nx / CW, a.nb);
-    k<<<grid, CW * a.nch, smem, st>>>(a);
-    return cudaGetLastError();
-}
-
-template <typename T>
-cudaError_t launch_ddz(const ZTab<T> &tb, int nch, int L, const T *var, T *dvar, int n1, int nz, const T *preset,
-                       const T *stretch, int filter, cudaStream_t st)
-{
-    constexpr int CW = ColCfg<T>::CW, LMAX = ColCfg<T>::LMAX;
-    if (L > LMAX || nch > ColCfg<T>::MAXNCH || n1 <= 0) return cudaErrorInvalidValue;
-    const size_t smem = ((size_t)nz * CW + (size_t)2 * nch * CW) * sizeof(T);
-    auto k = ddz_kernel<T, CW, LMAX>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((n1 + CW - 1) / CW);
-    k<<<grid, CW * nch, smem, st>>>(tb, nch, L, var, dvar, n1, nz, preset, stretch, filter);
-    return cudaGetLastError();
-}
-
 // Kernel integral, z-derivatives and FP64 accumulation of one record pair (kernels.f90:293-358):
 //   kc  += div(f_xi) div(a_v),  kvx += d_x f_vx a_vx + d_x f_vz a_vz,
 //   kvz += d_z f_vx a_vx + d_z f_vz a_vz,  hes += f_acc_x^2 + f_acc_z^2,
@@ -547,7 +503,7 @@ __device__ __forceinline__ void kacc_dz(const KAccArgs<T> &a, const T *src, T *B
 }
 
 template <typename T, int CW, int LMAX>
-__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) kacc_col_kernel(KAccArgs<T> a)
+__global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, (min_blocks<T, CW>())) kacc_col_kernel(KAccArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *B0 = reinterpret_cast<T *>(smem_raw);
@@ -596,13 +552,10 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, ColCfg<T>::MINB) kacc_c
 template <typename T>
 cudaError_t launch_kacc_row(const KAccArgs<T> &a, cudaStream_t st);
 
-template <typename T>
-cudaError_t launch_kacc(const KAccArgs<T> &a, cudaStream_t st)
+template <typename T, int CW>
+static cudaError_t launch_kacc_cw(const KAccArgs<T> &a, cudaStream_t st)
 {
-    constexpr int CW = ColCfg<T>::CW, LMAX = ColCfg<T>::LMAX;
-    if (a.nx % CW || a.L > LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
-    cudaError_t e = launch_kacc_row<T>(a, st);
-    if (e != cudaSuccess) return e;
+    constexpr int LMAX = ColCfg<T>::LMAX;
     const size_t smem = ((size_t)2 * a.nz * CW + (size_t)2 * a.nch * CW) * sizeof(T);
     auto k = kacc_col_kernel<T, CW, LMAX>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -610,8 +563,76 @@ cudaError_t launch_kacc(const KAccArgs<T> &a, cudaStream_t st)
     k<<<grid, CW * a.nch, smem, st>>>(a);
     return cudaGetLastError();
 }
+
+template <typename T>
+cudaError_t launch_kacc(const KAccArgs<T> &a, cudaStream_t st)
+{
+    if (a.nx % a.colw || a.L > ColCfg<T>::LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
+    cudaError_t e = launch_kacc_row<T>(a, st);
+    if (e != cudaSuccess) return e;
+    return a.colw == 32 ? launch_kacc_cw<T, 32>(a, st) : launch_kacc_cw<T, 8>(a, st);
+}
 template cudaError_t launch_kacc<float>(const KAccArgs<float> &, cudaStream_t);
 template cudaError_t launch_kacc<double>(const KAccArgs<double> &, cudaStream_t);
+
+template <typename T, int CW>
+static cudaError_t launch_col_stage_cw(const StepArgs<T> &a, cudaStream_t st)
+{
+    constexpr int LMAX = ColCfg<T>::LMAX;
+    const size_t smem = ((size_t)2 * a.nz * CW + (size_t)8 * a.nch * CW) * sizeof(T);
+    auto k = col_stage_kernel<T, CW, LMAX>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid(a.nx / CW, a.nb);
+    k<<<grid, CW * a.nch, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_col_stage(const StepArgs<T> &a, cudaStream_t st)
+{
+    if (a.nx % a.colw || a.L > ColCfg<T>::LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
+    return a.colw == 32 ? launch_col_stage_cw<T, 32>(a, st) : launch_col_stage_cw<T, 8>(a, st);
+}
+
+template <typename T, int CW>
+static cudaError_t launch_end_step_cw(const StepArgs<T> &a, cudaStream_t st)
+{
+    constexpr int LMAX = ColCfg<T>::LMAX;
+    const size_t smem = (size_t)a.nz * CW * sizeof(T) * (a.ALO ? 2 : 1);
+    auto k = end_step_kernel<T, CW, LMAX>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid(a.nx / CW, a.nb);
+    k<<<grid, CW * a.nch, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_end_step(const StepArgs<T> &a, cudaStream_t st)
+{
+    if (a.nx % a.colw || a.L > ColCfg<T>::LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
+    return a.colw == 32 ? launch_end_step_cw<T, 32>(a, st) : launch_end_step_cw<T, 8>(a, st);
+}
+
+template <typename T, int CW>
+static cudaError_t launch_ddz_cw(const ZTab<T> &tb, int nch, int L, const T *var, T *dvar, int n1, int nz,
+                                 const T *preset, const T *stretch, int filter, cudaStream_t st)
+{
+    constexpr int LMAX = ColCfg<T>::LMAX;
+    const size_t smem = ((size_t)nz * CW + (size_t)2 * nch * CW) * sizeof(T);
+    auto k = ddz_kernel<T, CW, LMAX>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((n1 + CW - 1) / CW);
+    k<<<grid, CW * nch, smem, st>>>(tb, nch, L, var, dvar, n1, nz, preset, stretch, filter);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_ddz(const ZTab<T> &tb, int nch, int L, const T *var, T *dvar, int n1, int nz, const T *preset,
+                       const T *stretch, int filter, cudaStream_t st)
+{
+    if (L > ColCfg<T>::LMAX || nch > ColCfg<T>::MAXNCH || n1 <= 0) return cudaErrorInvalidValue;
+    return launch_ddz_cw<T, 8>(tb, nch, L, var, dvar, n1, nz, preset, stretch, filter, st);
+}
 
 template cudaError_t launch_col_stage<float>(const StepArgs<float> &, cudaStream_t);
 template cudaError_t launch_col_stage<double>(const StepArgs<double> &, cudaStream_t);

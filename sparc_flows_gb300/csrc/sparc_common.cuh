@@ -57,6 +57,7 @@ struct StepArgs {
     int *d_time;
     int src_until, k_inj, k_obs, steps_out;
     int filt_k0, filt_xall;  // FILTER_VARS_2D coverage (rows from filt_k0, all columns if filt_xall)
+    int colw;                // column-pass block width (8 or 32 columns)
     const T *inj_scale, *src_rows;
     int nrows;
     const double *src_w;
@@ -292,6 +293,7 @@ struct KAccArgs {
     T stretchx;
     ZTab<T> z1;
     int nch, L;
+    int colw;
 };
 template <typename T>
 cudaError_t launch_kacc(const KAccArgs<T> &k, cudaStream_t st);

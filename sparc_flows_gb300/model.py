@@ -193,7 +193,8 @@ def workload(name: str):
     """Return (RunConfig, model, list[SourceSpec], psi or None, cmul or None) for a workload.
 
     plain64   : nx=256 over 200 Mm, nz=300 polytrope, no flow, 1 source, 1800 steps (FP64 plain).
-    autograd32: nx=512 over 400 Mm, supergranule psi flow (vx peak 240 m/s), 1 source, 3600 steps.
+    autograd32: nx=512 over 400 Mm, supergranule psi flow (vx peak 240 m/s), 1 source, 3600 steps,
+                20-layer bottom PML (10 at the top).
     batch32   : as autograd32 with 32 sources at x = -200 + 12.5 (s + 0.5) Mm and a 5 % Gaussian
                 sound-speed bump (sigma 5 Mm at -3 Mm), 3600 steps.
     """
@@ -201,7 +202,10 @@ def workload(name: str):
     if name == "plain64":
         run = RunConfig(nx=256, nz=300, xlength_cm=200e8, nsteps=1800, flows=False)
         return run, model, [SourceSpec(0.0)], None, None
-    run = RunConfig(nx=512, nz=300, xlength_cm=400e8, nsteps=3600, flows=True)
+    # 20 bottom PML layers: with 10, the bottom PML of this polytrope (CFL 0.8 where c is largest)
+    # carries a mode growing 0.4 % per step, which FP32 rounding seeds at 1e-7 and brings to O(1)
+    # within 3600 steps; from 15 layers on it decays (measured with the FP64 oracle).
+    run = RunConfig(nx=512, nz=300, xlength_cm=400e8, nsteps=3600, flows=True, npmlbot=20)
     amp = psi_amplitude_for_peak(run, model, 240.0)
     psi = gaussian_psi(run, model, amp)
     if name == "autograd32":

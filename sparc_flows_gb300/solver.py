@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
 
 import numpy as np
 import torch
@@ -123,6 +124,8 @@ class WaveSolver:
         cfg.flows, cfg.c2d, cfg.bg_per_solve = int(self.flows), int(c2d), int(per_solve)
         cfg.steps_out, cfg.k_inj, cfg.k_obs, cfg.src_until = run.steps_out, k_inj, self.o_rad, run.src_until
         cfg.filter_k0, cfg.filter_all_x = run.filter_kst - 1, int(run.filter_all_x)
+        cfg.compensated = int(os.environ.get("SPARC_COMPENSATED", "1"))
+        cfg.column_block = int(os.environ.get("SPARC_COLUMN_BLOCK", "32"))
         self.cfg = cfg
         h = ctypes.c_void_p()
         capi.check(self.L.sparc_plan_create(ctypes.byref(cfg), ctypes.byref(h)), "sparc_plan_create")
