@@ -56,6 +56,7 @@ typedef struct {
                                   update and filter round like FP64 arithmetic (no reference
                                   counterpart; the reference state is FP64) */
     int column_block;          /* column-pass block width: 32 or 8 x-columns (tuning) */
+    int column_impl;           /* 1: column pass with TMA-staged tiles (default), 0: direct loads */
 } sparc_config_t;
 
 /* Background, all DEVICE pointers to FP64 arrays; copied (and rounded for FP32 plans) into

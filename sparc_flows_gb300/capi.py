@@ -53,7 +53,7 @@ class SparcConfig(ctypes.Structure):
         ("flows", ctypes.c_int), ("c2d", ctypes.c_int), ("bg_per_solve", ctypes.c_int),
         ("steps_out", ctypes.c_int), ("k_inj", ctypes.c_int), ("k_obs", ctypes.c_int), ("src_until", ctypes.c_int),
         ("filter_k0", ctypes.c_int), ("filter_all_x", ctypes.c_int), ("compensated", ctypes.c_int),
-        ("column_block", ctypes.c_int),
+        ("column_block", ctypes.c_int), ("column_impl", ctypes.c_int),
     ]
 
 

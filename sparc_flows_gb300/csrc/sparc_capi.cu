@@ -10,8 +10,12 @@
 #include <vector>
 #include <algorithm>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "sparc_common.cuh"
 #include "sparc_gb300.h"
+#include "sparc_tma.cuh"
 
 using namespace sparc;
 
@@ -303,9 +307,34 @@ cudaError_t upload_fft(int n, DevFFT<T> &d, std::vector<void *> &allocs)
     return e;
 }
 
+// 2-D tiled tensor map over rows x nx of an x-fastest field array (box: 8 columns x boxr rows).
+bool encode_map(CUtensorMap *m, const void *base, int nx, long long rows, int boxr, size_t esize)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return false;
+        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)nx * esize};
+    const cuuint32_t box[2] = {8u, (cuuint32_t)boxr};
+    const cuuint32_t estr[2] = {1u, 1u};
+    CUresult r = encode(m, esize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2,
+                        const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 template <typename T>
 struct Solver {
     StepArgs<T> a{};
+    ColMaps maps{};
+    bool have_maps = false;
     DevZ<T> z[4];
     DevFFT<T> fft;
     std::vector<void *> allocs;
@@ -325,6 +354,7 @@ struct sparc_plan {
     Solver<float> s32;
     Solver<double> s64;
     int *d_time = nullptr;
+    int *d_err = nullptr;
     bool have_bg = false, have_src = false;
     double unstretch_top = 1.0;
     cudaGraphExec_t gexec = nullptr;
@@ -416,6 +446,29 @@ int alloc_solver(sparc_plan *p)
     a.filt_k0 = c.filter_k0; a.filt_xall = c.filter_all_x;
     a.colw = (c.column_block == 32 && nx % 32 == 0) ? 32 : 8;
     a.inj_scale = inj; a.src_rows = rows; a.nrows = 1;
+    a.d_err = p->d_err;
+    // TMA tiles: boxes of boxr rows, a multiple of 128 bytes so both boxes of a tile start
+    // 128-byte aligned in shared memory; two boxes cover nz
+    {
+        const int per128 = (int)(128 / (8 * sizeof(T)));
+        int boxr = (nz + 1) / 2;
+        boxr = ((boxr + per128 - 1) / per128) * per128;
+        a.boxr = boxr;
+        const size_t es = sizeof(T);
+        S.have_maps = boxr <= 256 && nx % 8 == 0 && c.column_impl != 0 &&
+                      encode_map(&S.maps.A, A, nx, (long long)nb * 4 * nz, boxr, es) &&
+                      encode_map(&S.maps.SV, SV, nx, (long long)3 * nb * 2 * nz, boxr, es) &&
+                      encode_map(&S.maps.DX, DX, nx, (long long)nb * nz, boxr, es) &&
+                      encode_map(&S.maps.FXX, FXX, nx, (long long)nb * nz, boxr, es) &&
+                      encode_map(&S.maps.FXZ, FXZ, nx, (long long)nb * nz, boxr, es);
+        if (S.have_maps) {
+            const size_t smem = col_tma_smem_bytes<T>(nz, p->nch, boxr);
+            int maxsm = 0, dev = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+            if (smem > (size_t)maxsm) S.have_maps = false;
+        }
+    }
     return SPARC_OK;
 }
 
@@ -424,6 +477,20 @@ void free_solver(Solver<T> &S)
 {
     for (void *q : S.allocs) cudaFree(q);
     S.allocs.clear();
+}
+
+template <typename T>
+cudaError_t col_stage(sparc_plan *p, const StepArgs<T> &a, cudaStream_t st)
+{
+    Solver<T> &S = solver<T>(p);
+    return S.have_maps ? launch_col_stage_tma<T>(S.maps, a, st) : launch_col_stage<T>(a, st);
+}
+
+template <typename T>
+cudaError_t end_step(sparc_plan *p, const StepArgs<T> &a, cudaStream_t st)
+{
+    Solver<T> &S = solver<T>(p);
+    return (S.have_maps && !a.ALO) ? launch_end_step_tma<T>(S.maps, a, st) : launch_end_step<T>(a, st);
 }
 
 template <typename T>
@@ -437,7 +504,7 @@ cudaError_t enqueue_step(sparc_plan *p, StepArgs<T> a, cudaStream_t st)
         a.bsm1 = (s >= 2) ? (T)B[s - 2] : T(0);
         a.slot_s = s % 3; a.slot_sm1 = (s - 1) % 3; a.slot_sm2 = (s + 1) % 3;  // (s-2) mod 3
         if ((e = launch_row_stage<T>(a, st)) != cudaSuccess) return e;
-        if ((e = launch_col_stage<T>(a, st)) != cudaSuccess) return e;
+        if ((e = col_stage(p, a, st)) != cudaSuccess) return e;
     }
     a.stage = 6;
     a.bs = (T)0; a.bsm1 = (T)B[4];
@@ -446,7 +513,7 @@ cudaError_t enqueue_step(sparc_plan *p, StepArgs<T> a, cudaStream_t st)
     a.stage = 7;
     a.bs = (T)B[4];
     a.slot_s = 5 % 3; a.slot_sm1 = 4 % 3;
-    return launch_end_step<T>(a, st);
+    return end_step(p, a, st);
 }
 
 template <typename T>
@@ -473,14 +540,14 @@ int profile_passes(sparc_plan *p, int nsteps, double *ms, cudaStream_t st)
             a.slot_s = s % 3; a.slot_sm1 = (s - 1) % 3; a.slot_sm2 = (s + 1) % 3;
             rec(0); e = launch_row_stage<T>(a, st); rec(-1);
             if (e != cudaSuccess) break;
-            rec(1); e = launch_col_stage<T>(a, st); rec(-1);
+            rec(1); e = col_stage(p, a, st); rec(-1);
         }
         if (e != cudaSuccess) break;
         a.stage = 6; a.bs = T(0); a.bsm1 = (T)B[4]; a.slot_s = 0; a.slot_sm1 = 2; a.slot_sm2 = 1;
         rec(0); e = launch_row_stage<T>(a, st); rec(-1);
         if (e != cudaSuccess) break;
         a.stage = 7; a.bs = (T)B[4]; a.slot_s = 2; a.slot_sm1 = 1;
-        rec(2); e = launch_end_step<T>(a, st); rec(-1);
+        rec(2); e = end_step(p, a, st); rec(-1);
     }
     cudaError_t es = cudaStreamSynchronize(st);
     ms[0] = ms[1] = ms[2] = ms[3] = 0.0;
@@ -675,6 +742,10 @@ int sparc_plan_create(const sparc_config_t *cfg, sparc_plan_t **out)
     cudaError_t e = cudaMalloc(&p->d_time, sizeof(int));
     if (e != cudaSuccess) { delete p; return fail(SPARC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e)); }
     p->allocs.push_back(p->d_time);
+    e = cudaMalloc(&p->d_err, sizeof(int));
+    if (e != cudaSuccess) { sparc_plan_destroy(p); return fail(SPARC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e)); }
+    p->allocs.push_back(p->d_err);
+    cudaMemset(p->d_err, 0, sizeof(int));
     int zero = -1;
     cudaMemcpy(p->d_time, &zero, sizeof(int), cudaMemcpyHostToDevice);
     for (int ibc = 0; ibc < 4; ibc++) {
@@ -814,6 +885,10 @@ int sparc_check_state(sparc_plan_t *p, double *norms, void *stream)
         norms[b] = std::sqrt(norms[b]);
         if (!std::isfinite(norms[b])) bad = true;
     }
+    int derr = 0;
+    CK(cudaMemcpy(&derr, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (derr == SPARC_DEV_ERR_TMA_TIMEOUT)
+        return fail(SPARC_ERR_TIMEOUT, "sparc_check_state: a bounded wait for staged column tiles gave up");
     if (bad) return fail(SPARC_ERR_NONFINITE, "sparc_check_state: non-finite v_z (the solve diverged)");
     return SPARC_OK;
 }

@@ -15,6 +15,7 @@ namespace sparc {
 
 constexpr int WARP = 32;
 constexpr int MAX_NCH = 24;  // chunks per column (nz <= MAX_NCH * LMAX)
+constexpr int SPARC_DEV_ERR_TMA_TIMEOUT = 1;  // device error flag: a bounded mbarrier wait gave up
 
 // Field order of the live state (xi_y and v_y vanish identically in 2-D).
 enum { F_XIX = 0, F_XIZ = 1, F_VX = 2, F_VZ = 3 };
@@ -58,6 +59,8 @@ struct StepArgs {
     int src_until, k_inj, k_obs, steps_out;
     int filt_k0, filt_xall;  // FILTER_VARS_2D coverage (rows from filt_k0, all columns if filt_xall)
     int colw;                // column-pass block width (8 or 32 columns)
+    int boxr;                // rows per TMA box of the staged column pass (2 boxes cover nz)
+    int *d_err;              // device error flag (SPARC_DEV_ERR_*)
     const T *inj_scale, *src_rows;
     int nrows;
     const double *src_w;
@@ -299,5 +302,13 @@ template <typename T>
 cudaError_t launch_kacc(const KAccArgs<T> &k, cudaStream_t st);
 
 bool fft_size_supported(int n);
+
+struct ColMaps;
+template <typename T>
+cudaError_t launch_col_stage_tma(const ColMaps &maps, const StepArgs<T> &a, cudaStream_t st);
+template <typename T>
+size_t col_tma_smem_bytes(int nz, int nch, int boxr);
+template <typename T>
+cudaError_t launch_end_step_tma(const ColMaps &maps, const StepArgs<T> &a, cudaStream_t st);
 
 }  // namespace sparc
