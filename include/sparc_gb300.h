@@ -55,8 +55,12 @@ typedef struct {
     int compensated;           /* FP32 plans: 1 keeps a low-order part of the state so the RK
                                   update and filter round like FP64 arithmetic (no reference
                                   counterpart; the reference state is FP64) */
-    int column_block;          /* column-pass block width: 32 or 8 x-columns (tuning) */
-    int column_impl;           /* 1: column pass with TMA-staged tiles (default), 0: direct loads */
+    int column_block;          /* column-pass block width in x-columns (tuning): 32 or 8 for the
+                                  partitioned solve (other values: 32), 32, 16 or 8 for the banded
+                                  pass (other values: 16) */
+    int column_impl;           /* column pass: 0 partitioned solve with direct loads, 1 partitioned
+                                  solve with TMA-staged tiles, 2 (FP32 plans) banded inverse of the
+                                  compact operator, FP64 plans then use 0 */
 } sparc_config_t;
 
 /* Background, all DEVICE pointers to FP64 arrays; copied (and rounded for FP32 plans) into
@@ -170,6 +174,13 @@ int sparc_kernels_accumulate(sparc_plan_t *plan, const void *fsn, int nfwd, int 
  * call writes every element it reads.  Same arguments and results as sparc_kernels_accumulate. */
 int sparc_kernels_accumulate_static(sparc_plan_t *plan, const void *fsn, int nfwd, int jf, double *out,
                                     void *stream);
+
+/* Host-only FP64 evaluation of the banded form of dbyd2 that FP32 plans use on the device:
+ * the right-hand side as dbyd2 forms it, then T^{-1} as a Toeplitz band of half-width 20 plus
+ * rank-2 corrections on the 24 x 24 corners (ibc 1..3; preset as in sparc_zsolve_host).
+ * *band_err (may be NULL) receives max |T^{-1} - band form| / max |T^{-1}|.  (dbyd2.f:8-235) */
+int sparc_zband_host(int nz, int ibc, const double *b, double *x, const double *preset, int n1,
+                     double *band_err);
 
 /* Host-only FP64 evaluation of the partitioned compact-derivative algebra that the device
  * code applies (no GPU needed): x[nz][n1] = dbyd2(b, ibc) without the stretch factor, with

@@ -173,6 +173,128 @@ bool build_ztab(int nz, int ibc, int nch, int L, HostZTab &t)
     return true;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Banded form of the compact derivative (FP32 column pass).  The right-hand side is formed
+// exactly as dbyd2 forms it; the tridiagonal solve x = T^{-1} rhs becomes a band sum.  Away
+// from the ends T is Toeplitz (1/3, 1, 1/3), whose inverse decays like r^|d|,
+// r = -(3 - sqrt 5)/2 = -0.382, so t[d] = T^{-1}[kc][kc+d] for |d| <= 20 holds the interior
+// rows to 3e-9 of t[0].  The boundary rows of T (dbyd2.f:151-196) and the finite ends leave a
+// correction T^{-1} - band that is confined to the two KC x KC corners (outside them it is below
+// 1e-9) and has rank 2 there; it is factored by cross approximation with full pivoting.
+// ---------------------------------------------------------------------------------------------
+struct HostBand {
+    int nz = 0, q = 0;
+    double t[BAND_W + 1] = {};
+    std::vector<double> uv;  // Ub [KC][Q], Vb [Q][KC], Ut [KC][Q], Vt [Q][KC]
+    double err = 0;          // max |T^{-1} - band - corners| / max |T^{-1}|
+};
+
+// Cross approximation of the n x n matrix C (row-major) to rank <= qmax: C ~ U V.
+static int cross_approx(std::vector<double> C, int n, int qmax, double tol, double *U, double *V)
+{
+    for (int i = 0; i < n * qmax; i++) { U[i] = 0.0; V[i] = 0.0; }
+    int q = 0;
+    for (; q < qmax; q++) {
+        int pi = 0, pj = 0;
+        double best = 0.0;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++)
+                if (std::fabs(C[(size_t)i * n + j]) > best) { best = std::fabs(C[(size_t)i * n + j]); pi = i; pj = j; }
+        if (best <= tol) break;
+        const double piv = C[(size_t)pi * n + pj];
+        for (int i = 0; i < n; i++) U[i * qmax + q] = C[(size_t)i * n + pj];
+        for (int j = 0; j < n; j++) V[q * n + j] = C[(size_t)pi * n + j] / piv;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) C[(size_t)i * n + j] -= U[i * qmax + q] * V[q * n + j];
+    }
+    return q;
+}
+
+bool build_band(const HostZTab &tz, HostBand &h)
+{
+    const int nz = tz.nz, W = BAND_W, KC = BAND_KC, Q = BAND_Q;
+    if (nz < 2 * KC + 2 * W) return false;
+    h.nz = nz;
+    // T^{-1} column by column (diag 1, sub lowr, super uppr), Thomas on unit vectors
+    std::vector<double> gam(nz), bet(nz), Ti((size_t)nz * nz, 0.0), y(nz);
+    bet[0] = 1.0;
+    for (int k = 1; k < nz; k++) {
+        gam[k] = tz.uppr[k - 1] / bet[k - 1];
+        bet[k] = 1.0 - tz.lowr[k] * gam[k];
+    }
+    for (int col = 0; col < nz; col++) {
+        for (int k = 0; k < nz; k++) y[k] = ((k == col ? 1.0 : 0.0) - (k > 0 ? tz.lowr[k] * y[k - 1] : 0.0)) / bet[k];
+        for (int k = nz - 2; k >= 0; k--) y[k] -= gam[k + 1] * y[k + 1];
+        for (int k = 0; k < nz; k++) Ti[(size_t)k * nz + col] = y[k];
+    }
+    const int kc = nz / 2;
+    for (int d = 0; d <= W; d++) h.t[d] = Ti[(size_t)kc * nz + kc + d];
+    auto band = [&](int k, int j) { const int d = std::abs(k - j); return d <= W ? h.t[d] : 0.0; };
+    double mx = 0.0;
+    for (double v : Ti) mx = std::max(mx, std::fabs(v));
+    h.uv.assign((size_t)4 * KC * Q, 0.0);
+    double *Ub = h.uv.data(), *Vb = Ub + KC * Q, *Ut = Vb + KC * Q, *Vt = Ut + KC * Q;
+    std::vector<double> C((size_t)KC * KC);
+    for (int i = 0; i < KC; i++)
+        for (int j = 0; j < KC; j++) C[(size_t)i * KC + j] = Ti[(size_t)i * nz + j] - band(i, j);
+    const int qb = cross_approx(C, KC, Q, 1e-13 * mx, Ub, Vb);
+    const int o = nz - KC;
+    for (int i = 0; i < KC; i++)
+        for (int j = 0; j < KC; j++) C[(size_t)i * KC + j] = Ti[(size_t)(o + i) * nz + o + j] - band(o + i, o + j);
+    const int qt = cross_approx(C, KC, Q, 1e-13 * mx, Ut, Vt);
+    h.q = std::max(qb, qt);
+    double dev = 0.0;
+    for (int k = 0; k < nz; k++)
+        for (int j = 0; j < nz; j++) {
+            double v = band(k, j);
+            if (k < KC && j < KC)
+                for (int q = 0; q < Q; q++) v += Ub[k * Q + q] * Vb[q * KC + j];
+            if (k >= o && j >= o)
+                for (int q = 0; q < Q; q++) v += Ut[(k - o) * Q + q] * Vt[q * KC + (j - o)];
+            dev = std::max(dev, std::fabs(Ti[(size_t)k * nz + j] - v));
+        }
+    h.err = dev / mx;
+    return h.err < 1e-8;
+}
+
+// dbyd2's right-hand side of row k of column i (interior c1/c2 differences, boundary closures,
+// caller-set row), the same algebra as zrhs on the device.
+static double zrhs_host(const HostZTab &t, const double *b, int n1, int i, int k, double preset)
+{
+    const int nz = t.nz;
+    auto f = [&](int kk) { return b[(size_t)kk * n1 + i]; };
+    if (k >= 2 && k <= nz - 3) return t.c1 * (f(k + 1) - f(k - 1)) + t.c2 * (f(k + 2) - f(k - 2));
+    if (k == t.preset_row) return preset;
+    const int base = (k <= 1) ? 0 : nz - 5;
+    double r = 0.0;
+    for (int j = 0; j < 5; j++) r += t.w5[(size_t)k * 5 + j] * f(base + j);
+    return r;
+}
+
+// Host evaluation of the banded form (same algebra as the device code), unstretched.
+void zband_host(const HostZTab &t, const HostBand &h, const double *b, double *x, const double *preset_v, int n1)
+{
+    const int nz = h.nz, W = BAND_W, KC = BAND_KC, Q = BAND_Q, o = nz - KC;
+    const double *Ub = h.uv.data(), *Vb = Ub + KC * Q, *Ut = Vb + KC * Q, *Vt = Ut + KC * Q;
+    std::vector<double> rhs(nz);
+    for (int i = 0; i < n1; i++) {
+        for (int k = 0; k < nz; k++) rhs[k] = zrhs_host(t, b, n1, i, k, preset_v ? preset_v[i] : 0.0);
+        double sb[BAND_Q] = {}, st[BAND_Q] = {};
+        for (int q = 0; q < Q; q++)
+            for (int j = 0; j < KC; j++) { sb[q] += Vb[q * KC + j] * rhs[j]; st[q] += Vt[q * KC + j] * rhs[o + j]; }
+        for (int k = 0; k < nz; k++) {
+            double v = 0.0;
+            for (int d = -W; d <= W; d++)
+                if (k + d >= 0 && k + d < nz) v += h.t[std::abs(d)] * rhs[k + d];
+            if (k < KC)
+                for (int q = 0; q < Q; q++) v += Ub[k * Q + q] * sb[q];
+            if (k >= o)
+                for (int q = 0; q < Q; q++) v += Ut[(k - o) * Q + q] * st[q];
+            x[(size_t)k * n1 + i] = v;
+        }
+    }
+}
+
 // Host evaluation of the partitioned solve (same algebra as the device code).
 void zsolve_host(const HostZTab &t, const double *b, double *x, const double *preset_v, int n1)
 {
@@ -337,6 +459,9 @@ struct Solver {
     bool have_maps = false;
     DevZ<T> z[4];
     DevFFT<T> fft;
+    BandDev band{};    // banded z-derivative tables (FP32 plans, column_impl 2)
+    int band_R = 0;    // rows per thread group of the banded column pass (0: not used)
+    int band_cw = 0;   // its block width (columns)
     std::vector<void *> allocs;
     size_t F = 0;
     T *work = nullptr;  // kernel-accumulation scratch [nb][8][nz][nx]
@@ -444,9 +569,36 @@ int alloc_solver(sparc_plan *p)
     a.d_time = p->d_time;
     a.src_until = c.src_until; a.k_inj = c.k_inj; a.k_obs = c.k_obs; a.steps_out = c.steps_out;
     a.filt_k0 = c.filter_k0; a.filt_xall = c.filter_all_x;
-    a.colw = (c.column_block == 32 && nx % 32 == 0) ? 32 : 8;
+    a.colw = (c.column_block != 8 && nx % 32 == 0) ? 32 : 8;
     a.inj_scale = inj; a.src_rows = rows; a.nrows = 1;
     a.d_err = p->d_err;
+    // banded column pass (FP32 only: its truncation at 5e-10 is below FP32 rounding, not FP64's)
+    S.band_R = 0;
+    const int bcw = (c.column_block == 8 || c.column_block == 16 || c.column_block == 32) ? c.column_block : 16;
+    if (sizeof(T) == 4 && c.column_impl == 2 && nx % bcw == 0 && col_band_rows(nz, bcw) > 0) {
+        const int R = col_band_rows(nz, bcw);
+        int maxsm = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        bool ok = col_band_smem_bytes(nz, R, bcw) <= (size_t)maxsm;
+        HostBand hb[3];
+        for (int i = 0; i < 3 && ok; i++) ok = build_band(p->hz[i + 1], hb[i]);
+        for (int i = 1; i < 3 && ok; i++)
+            for (int d = 0; d <= BAND_W; d++) ok = ok && std::fabs(hb[i].t[d] - hb[0].t[d]) <= 1e-12 * std::fabs(hb[0].t[0]);
+        for (int i = 0; i < 3 && ok; i++) {
+            std::vector<float> f(hb[i].uv.begin(), hb[i].uv.end());
+            void *ptr = nullptr;
+            if (cudaMalloc(&ptr, f.size() * sizeof(float)) != cudaSuccess) return fail(SPARC_ERR_CUDA, "cudaMalloc: band tables");
+            S.allocs.push_back(ptr);
+            cudaMemcpy(ptr, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
+            S.band.uv[i] = (const float *)ptr;
+        }
+        if (ok) {
+            for (int d = 0; d <= BAND_W; d++) S.band.t[d] = (float)hb[0].t[d];
+            S.band_R = R;
+            S.band_cw = bcw;
+        }
+    }
     // TMA tiles: boxes of boxr rows, a multiple of 128 bytes so both boxes of a tile start
     // 128-byte aligned in shared memory; two boxes cover nz
     {
@@ -483,7 +635,22 @@ template <typename T>
 cudaError_t col_stage(sparc_plan *p, const StepArgs<T> &a, cudaStream_t st)
 {
     Solver<T> &S = solver<T>(p);
-    return S.have_maps ? launch_col_stage_tma<T>(S.maps, a, st) : launch_col_stage<T>(a, st);
+    if constexpr (sizeof(T) == 4) {
+        switch (S.band_cw * 100 + S.band_R) {
+            case 3208: return launch_col_stage_band<32, 8>(a, S.band, st);
+            case 3210: return launch_col_stage_band<32, 10>(a, S.band, st);
+            case 3212: return launch_col_stage_band<32, 12>(a, S.band, st);
+            case 1609: return launch_col_stage_band<16, 9>(a, S.band, st);
+            case 1611: return launch_col_stage_band<16, 11>(a, S.band, st);
+            case 1613: return launch_col_stage_band<16, 13>(a, S.band, st);
+            case 809: return launch_col_stage_band<8, 9>(a, S.band, st);
+            case 811: return launch_col_stage_band<8, 11>(a, S.band, st);
+            case 813: return launch_col_stage_band<8, 13>(a, S.band, st);
+            default: break;
+        }
+    }
+    return (S.have_maps && p->cfg.column_impl == 1) ? launch_col_stage_tma<T>(S.maps, a, st)
+                                                     : launch_col_stage<T>(a, st);
 }
 
 template <typename T>
@@ -1016,6 +1183,19 @@ int sparc_kernels_accumulate_static(sparc_plan_t *p, const void *fsn, int nfwd, 
 
 // Host evaluation of the partitioned compact-derivative tables (FP64), the same algebra the
 // device code applies; used to validate the tables without a GPU.
+int sparc_zband_host(int nz, int ibc, const double *b, double *x, const double *preset, int n1, double *band_err)
+{
+    if (!b || !x || n1 < 1 || ibc < 1 || ibc > 3) return fail(SPARC_ERR_ARG, "sparc_zband_host: bad argument");
+    int nch, L;  // chunk factors are not used by the band form
+    if (!chunking(nz, std::max(16, (nz + 19) / 20), nch, L)) return fail(SPARC_ERR_SIZE, "sparc_zband_host: bad size");
+    HostZTab t;
+    HostBand h;
+    if (!build_ztab(nz, ibc, nch, L, t) || !build_band(t, h)) return fail(SPARC_ERR_SIZE, "sparc_zband_host: no band form");
+    if (band_err) *band_err = h.err;
+    zband_host(t, h, b, x, preset, n1);
+    return SPARC_OK;
+}
+
 int sparc_zsolve_host(int nz, int ibc, int lmax, const double *b, double *x, const double *preset, int n1)
 {
     if (!b || !x || n1 < 1 || ibc < 0 || ibc > 3) return fail(SPARC_ERR_ARG, "sparc_zsolve_host: bad argument");

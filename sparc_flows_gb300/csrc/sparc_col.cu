@@ -32,20 +32,6 @@ struct ColCfg<double> {
 template <typename T, int CW>
 constexpr int min_blocks() { return CW <= 8 ? (sizeof(T) == 4 ? 4 : 2) : 1; }
 
-template <typename T>
-__device__ __forceinline__ T *svp(const StepArgs<T> &a, int slot, int b, int c)
-{
-    return a.SV + (((size_t)slot * a.nb + b) * 2 + c) * (size_t)a.nz * a.nx;
-}
-
-template <typename T>
-__device__ __forceinline__ int pml_row(const StepArgs<T> &a, int k)
-{
-    if (k < a.npmlbot) return k;
-    if (k >= a.nz - a.npmltop) return a.npmlbot + (k - (a.nz - a.npmltop));
-    return -1;
-}
-
 template <typename T, int CW, int LMAX>
 __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, (min_blocks<T, CW>())) col_stage_kernel(StepArgs<T> a)
 {

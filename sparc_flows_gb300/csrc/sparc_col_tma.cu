@@ -18,20 +18,6 @@ constexpr int TMA_NTILE = 9;
 constexpr uint32_t TMA_WAIT_ITERS = 1u << 24;
 
 template <typename T>
-__device__ __forceinline__ T *svp_t(const StepArgs<T> &a, int slot, int b, int c)
-{
-    return a.SV + (((size_t)slot * a.nb + b) * 2 + c) * (size_t)a.nz * a.nx;
-}
-
-template <typename T>
-__device__ __forceinline__ int pml_row_t(const StepArgs<T> &a, int k)
-{
-    if (k < a.npmlbot) return k;
-    if (k >= a.nz - a.npmltop) return a.npmlbot + (k - (a.nz - a.npmltop));
-    return -1;
-}
-
-template <typename T>
 __global__ void __launch_bounds__(TMA_CW * 20, (sizeof(T) == 4 ? 2 : 1))
     col_stage_tma_kernel(const __grid_constant__ ColMaps maps, StepArgs<T> a)
 {
@@ -129,7 +115,7 @@ __global__ void __launch_bounds__(TMA_CW * 20, (sizeof(T) == 4 ? 2 : 1))
                 const int k = k0 + m, q = k * CW + c;
                 const size_t g = (size_t)k * nx + x;
                 T dzz = zcorrect(a.z3, y[m], k, xl, xr) * __ldg(a.stretch + k);
-                const int pi = pml_row_t(a, k);
+                const int pi = pml_row(a, k);
                 T fd = T(1);
                 if (pi >= 0) {
                     const size_t qz = ((size_t)b * 2 * a.nzpml + pi) * nx + x;
@@ -177,7 +163,7 @@ __global__ void __launch_bounds__(TMA_CW * 20, (sizeof(T) == 4 ? 2 : 1))
                 const int k = k0 + m, q = k * CW + c;
                 const size_t g = (size_t)k * nx + x;
                 T gpz = zcorrect(a.z2, y[m], k, xl, xr) * __ldg(a.stretch + k);
-                const int pi = pml_row_t(a, k);
+                const int pi = pml_row(a, k);
                 if (pi >= 0) {
                     const size_t qz = (((size_t)b * 2 + 1) * a.nzpml + pi) * nx + x;
                     const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
@@ -222,7 +208,7 @@ __global__ void __launch_bounds__(TMA_CW * 20, (sizeof(T) == 4 ? 2 : 1))
         }
         forcing = T(f) * __ldg(a.inj_scale + (size_t)b * nx + x);
     }
-    T *svz = svp_t(a, a.slot_s, b, 1);
+    T *svz = svp(a, a.slot_s, b, 1);
 #pragma unroll
     for (int m = 0; m < LMAX; m++) {
         if (m < n) {
@@ -359,7 +345,7 @@ __global__ void __launch_bounds__(TMA_CW * 20, (sizeof(T) == 4 ? 2 : 1))
     for (int m = 0; m < n; m++) {
         const int k = k0 + m;
         const size_t g = (size_t)k * nx + x;
-        const int pi = pml_row_t(a, k);
+        const int pi = pml_row(a, k);
         if (pi >= 0) {
             for (int cc = 0; cc < 2; cc++) {
                 const size_t qz = (((size_t)b * 2 + cc) * a.nzpml + pi) * nx + x;

@@ -16,6 +16,9 @@ namespace sparc {
 constexpr int WARP = 32;
 constexpr int MAX_NCH = 24;  // chunks per column (nz <= MAX_NCH * LMAX)
 constexpr int SPARC_DEV_ERR_TMA_TIMEOUT = 1;  // device error flag: a bounded mbarrier wait gave up
+// Banded form of the compact z-derivative (FP32 column pass): T^{-1} as a symmetric Toeplitz
+// band of half-width BAND_W plus rank-BAND_Q corrections on the BAND_KC x BAND_KC corners.
+constexpr int BAND_W = 20, BAND_KC = 24, BAND_Q = 3;
 
 // Field order of the live state (xi_y and v_y vanish identically in 2-D).
 enum { F_XIX = 0, F_XIZ = 1, F_VX = 2, F_VZ = 3 };
@@ -70,14 +73,41 @@ struct StepArgs {
     int nrec_cap;
 };
 
+template <typename T>
+__device__ __forceinline__ T *svp(const StepArgs<T> &a, int slot, int b, int c)
+{
+    return a.SV + (((size_t)slot * a.nb + b) * 2 + c) * (size_t)a.nz * a.nx;
+}
+
+// Row of the vertical-PML arrays holding depth row k (-1 outside both layers).
+template <typename T>
+__device__ __forceinline__ int pml_row(const StepArgs<T> &a, int k)
+{
+    if (k < a.npmlbot) return k;
+    if (k >= a.nz - a.npmltop) return a.npmlbot + (k - (a.nz - a.npmltop));
+    return -1;
+}
+
+// Banded compact-derivative tables (FP32 plans).  x = T^{-1} rhs is evaluated as
+//   x[k] = sum_{|d| <= BAND_W} t[|d|] rhs[k+d]        (rhs zero outside 0..nz-1)
+//        + sum_q Ub[k][q] (Vb[q] . rhs[0..KC))         for k < KC
+//        + sum_q Ut[k'][q] (Vt[q] . rhs[nz-KC..nz))    for k' = k - (nz-KC) >= 0
+// uv[i] (boundary condition i+1) holds Ub [KC][Q], Vb [Q][KC], Ut [KC][Q], Vt [Q][KC].
+struct BandDev {
+    float t[BAND_W + 1];
+    const float *uv[3];
+};
+
 // ------------------------------------------------------------------------------------------
 // FFT
 // ------------------------------------------------------------------------------------------
+// Radix plan: as many radix-8 passes as possible, then 4, 2, 3 (512 = 8.8.8, 384 = 8.8.2.3).
 template <int N>
 struct Radices {
     static constexpr int count()
     {
         int n = N, c = 0;
+        while (n % 8 == 0) { n /= 8; c++; }
         while (n % 4 == 0) { n /= 4; c++; }
         while (n % 2 == 0) { n /= 2; c++; }
         while (n % 3 == 0) { n /= 3; c++; }
@@ -86,6 +116,7 @@ struct Radices {
     static constexpr int at(int i)
     {
         int n = N, c = 0;
+        while (n % 8 == 0) { if (c == i) return 8; n /= 8; c++; }
         while (n % 4 == 0) { if (c == i) return 4; n /= 4; c++; }
         while (n % 2 == 0) { if (c == i) return 2; n /= 2; c++; }
         while (n % 3 == 0) { if (c == i) return 3; n /= 3; c++; }
@@ -94,7 +125,7 @@ struct Radices {
 };
 
 template <typename T, int R>
-__device__ __forceinline__ void butterfly(T *vr, T *vi, bool inv)
+__host__ __device__ __forceinline__ void butterfly(T *vr, T *vi, bool inv)
 {
     if constexpr (R == 2) {
         T ar = vr[0], ai = vi[0];
@@ -110,6 +141,32 @@ __device__ __forceinline__ void butterfly(T *vr, T *vi, bool inv)
         vr[1] = d0r + jr;  vi[1] = d0i + ji;
         vr[2] = s0r - s1r; vi[2] = s0i - s1i;
         vr[3] = d0r - jr;  vi[3] = d0i - ji;
+    } else if constexpr (R == 8) {
+        // out[2q] = DFT4(v_k + v_{k+4})[q], out[2q+1] = DFT4((v_k - v_{k+4}) W8^k)[q]
+        const T r2 = T(0.7071067811865475244008443621048490);
+        T ar[4], ai[4], br[4], bi[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            ar[k] = vr[k] + vr[k + 4]; ai[k] = vi[k] + vi[k + 4];
+            br[k] = vr[k] - vr[k + 4]; bi[k] = vi[k] - vi[k + 4];
+        }
+        // W8^1 = (1 -/+ i)/sqrt2, W8^2 = -/+ i, W8^3 = (-1 -/+ i)/sqrt2 (forward / inverse)
+        const T sg = inv ? T(1) : T(-1);
+        {
+            T xr = br[1], xi = bi[1];
+            br[1] = r2 * (xr - sg * xi); bi[1] = r2 * (xi + sg * xr);
+            xr = br[2]; xi = bi[2];
+            br[2] = -sg * xi; bi[2] = sg * xr;
+            xr = br[3]; xi = bi[3];
+            br[3] = r2 * (-xr - sg * xi); bi[3] = r2 * (-xi + sg * xr);
+        }
+        butterfly<T, 4>(ar, ai, inv);
+        butterfly<T, 4>(br, bi, inv);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            vr[2 * q] = ar[q]; vi[2 * q] = ai[q];
+            vr[2 * q + 1] = br[q]; vi[2 * q + 1] = bi[q];
+        }
     } else {  // R == 3
         const T h = T(0.8660254037844386467637231707529362);
         T tr = vr[1] + vr[2], ti = vi[1] + vi[2];
@@ -123,12 +180,13 @@ __device__ __forceinline__ void butterfly(T *vr, T *vi, bool inv)
     }
 }
 
-// One Stockham autosort stage of radix R after NS points have been combined.
+// One Stockham autosort stage of radix R after NS points have been combined.  The first stage
+// (NS == 1) multiplies the real and imaginary inputs by sr and si.
 template <typename T, int N, int R, int NS>
 __device__ __forceinline__ void stockham_stage(const T *__restrict__ xr, const T *__restrict__ xi,
                                                T *__restrict__ yr, T *__restrict__ yi,
                                                const T *__restrict__ twr, const T *__restrict__ twi,
-                                               int lane, bool inv)
+                                               int lane, bool inv, T sr, T si)
 {
     constexpr int NR = N / R;
     constexpr int TS = N / (NS * R);
@@ -139,7 +197,9 @@ __device__ __forceinline__ void stockham_stage(const T *__restrict__ xr, const T
 #pragma unroll
         for (int r = 0; r < R; r++) {
             T ar = xr[j + r * NR], ai = xi[j + r * NR];
-            if (NS == 1 || r == 0) {
+            if (NS == 1) {
+                vr[r] = ar * sr; vi[r] = ai * si;
+            } else if (r == 0) {
                 vr[r] = ar; vi[r] = ai;
             } else {
                 const int t = r * k * TS;  // < N
@@ -162,29 +222,67 @@ __device__ __forceinline__ void stockham_stage(const T *__restrict__ xr, const T
 template <typename T, int N, int I, int NS>
 struct FFTRun {
     __device__ static __forceinline__ void run(T *xr, T *xi, T *yr, T *yi, const T *twr, const T *twi,
-                                               int lane, bool inv, T *&outr, T *&outi)
+                                               int lane, bool inv, T sr, T si, T *&outr, T *&outi)
     {
         if constexpr (I == Radices<N>::count()) {
             outr = xr; outi = xi;
         } else {
             constexpr int R = Radices<N>::at(I);
-            stockham_stage<T, N, R, NS>(xr, xi, yr, yi, twr, twi, lane, inv);
+            stockham_stage<T, N, R, NS>(xr, xi, yr, yi, twr, twi, lane, inv, sr, si);
             __syncwarp();
-            FFTRun<T, N, I + 1, NS * R>::run(yr, yi, xr, xi, twr, twi, lane, inv, outr, outi);
+            FFTRun<T, N, I + 1, NS * R>::run(yr, yi, xr, xi, twr, twi, lane, inv, T(1), T(1), outr, outi);
         }
     }
 };
 
+// Power of two 2^-e with e the binary exponent of the maximum m of |v| over a row
+// (m in [2^(e-1), 2^e)): scales the row's largest value into [0.5, 1) exactly.  Two real rows
+// packed in one complex FFT share its rounding, which is relative to the larger row; in FP32 a
+// row 1e7 times smaller than its partner (pressure against displacement at the bottom of a
+// polytrope) would keep no significant digit.  Scaling each row first makes the rounding
+// relative to the row itself.  The exponent is read from the bit pattern and the scale is kept
+// a normal number (subnormal rows get the largest scale, 2^125 / 2^1021); zero and non-finite
+// rows keep scale 1.
+__device__ __forceinline__ float pow2_scale_of(float m)
+{
+    if (!(m > 0.f) || !isfinite(m)) return 1.f;
+    const int E = (int)((__float_as_uint(m) >> 23) & 0xffu);  // biased exponent, 0 for subnormal
+    const int f = min(max(253 - max(E, 1), 1), 254);          // biased exponent of 2^(126 - E)
+    return __uint_as_float((unsigned)f << 23);
+}
+__device__ __forceinline__ double pow2_scale_of(double m)
+{
+    if (!(m > 0.0) || !isfinite(m)) return 1.0;
+    const int E = (int)((__double_as_longlong(m) >> 52) & 0x7ff);
+    const long long f = min(max(2045 - max(E, 1), 1), 2046);  // biased exponent of 2^(1022 - E)
+    return __longlong_as_double(f << 52);
+}
+// Scale s for a row whose lane-local max |v| is m_lane, and the factor that takes the FFT
+// output back (1/s, exact).  A row that is zero gets output factor 0: its partner, scaled to
+// O(1), leaks rounding of O(eps) into it, while its derivative is exactly zero.  (A NaN in such
+// a row still propagates: 0 * NaN is NaN.)
+template <typename T>
+__device__ __forceinline__ void warp_row_scale(T m_lane, T &s, T &inv)
+{
+    T m = m_lane;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    s = pow2_scale_of(m);
+    inv = (m == T(0)) ? T(0) : T(1) / s;
+}
+
 // Spectral derivative of the complex row (xr + i xi) of length N held in warp-private shared
-// memory (yr, yi are scratch of the same size): forward FFT, multiply bin k by
-// i*kap[k]*scale (kap already carries the 1/N normalisation and a zero Nyquist bin), inverse
-// FFT.  Real and imaginary parts of the result are the derivatives of the two real rows.
+// memory (yr, yi are scratch of the same size): forward FFT of (sr xr + i si xi), multiply bin
+// k by i*kap[k]*scale (kap already carries the 1/N normalisation and a zero Nyquist bin),
+// inverse FFT.  Real and imaginary parts of the result are the derivatives of the two real rows
+// times sr and si (powers of two from warp_row_scale; 1 for no scaling).
 template <typename T, int N>
 __device__ __forceinline__ void fft_deriv(T *xr, T *xi, T *yr, T *yi, const T *twr, const T *twi,
-                                          const T *kap, T scale, int lane, T *&outr, T *&outi)
+                                          const T *kap, T scale, int lane, T *&outr, T *&outi,
+                                          T sr = T(1), T si = T(1))
 {
     T *fr, *fi;
-    FFTRun<T, N, 0, 1>::run(xr, xi, yr, yi, twr, twi, lane, false, fr, fi);
+    FFTRun<T, N, 0, 1>::run(xr, xi, yr, yi, twr, twi, lane, false, sr, si, fr, fi);
     for (int k = lane; k < N; k += WARP) {
         T kk = __ldg(kap + k) * scale;
         T re = fr[k], im = fi[k];
@@ -193,7 +291,7 @@ __device__ __forceinline__ void fft_deriv(T *xr, T *xi, T *yr, T *yi, const T *t
     }
     __syncwarp();
     T *gr = (fr == xr) ? yr : xr, *gi = (fr == xr) ? yi : xi;
-    FFTRun<T, N, 0, 1>::run(fr, fi, gr, gi, twr, twi, lane, true, outr, outi);
+    FFTRun<T, N, 0, 1>::run(fr, fi, gr, gi, twr, twi, lane, true, T(1), T(1), outr, outi);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -302,6 +400,11 @@ template <typename T>
 cudaError_t launch_kacc(const KAccArgs<T> &k, cudaStream_t st);
 
 bool fft_size_supported(int n);
+
+template <int CW, int R>
+cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st);
+size_t col_band_smem_bytes(int nz, int R, int cw);
+int col_band_rows(int nz, int cw);  // rows per thread group (0: no banded pass for this depth / width)
 
 struct ColMaps;
 template <typename T>

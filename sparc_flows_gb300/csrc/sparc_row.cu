@@ -14,12 +14,6 @@ namespace sparc {
 
 constexpr int ROW_WPB = 4;  // rows (warps) per block
 
-template <typename T>
-__device__ __forceinline__ T *svp(const StepArgs<T> &a, int slot, int b, int c)
-{
-    return a.SV + (((size_t)slot * a.nb + b) * 2 + c) * (size_t)a.nz * a.nx;
-}
-
 // MODE 0: stage 1 (no pressure yet), MODE 1: stages 2..5, MODE 2: closing pass after stage 5.
 template <typename T, int N, int MODE>
 __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
@@ -43,6 +37,7 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
     const T *bxk = a.bx + (size_t)b * a.bgx + (size_t)k * nhx;
 
     // ---- load: (p_{s-1}, xi_x at stage s) or (p_5, 0)
+    T mr = T(0), mi = T(0);
     for (int x = lane; x < nx; x += WARP) {
         T p = T(0), xis = T(0);
         if (MODE != 0) p = __ldg(a.P + (size_t)b * F + ro + x);
@@ -56,14 +51,20 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
         }
         xr[x] = p;
         xi[x] = xis;
+        mr = fmax(mr, fabs(p));
+        mi = fmax(mi, fabs(xis));
     }
+    T sr, si, isr, isi;
+    warp_row_scale(mr, sr, isr);
+    warp_row_scale(mi, si, isi);
     __syncwarp();
     T *o1r, *o1i;
-    fft_deriv<T, N>(xr, xi, yr, yi, a.twr, a.twi, a.kap, a.stretchx, lane, o1r, o1i);
+    fft_deriv<T, N>(xr, xi, yr, yi, a.twr, a.twi, a.kap, a.stretchx, lane, o1r, o1i, sr, si);
     __syncwarp();
 
+    T mr2 = T(0), mi2 = T(0);
     for (int x = lane; x < nx; x += WARP) {
-        T gpx = o1r[x], dxx = o1i[x];
+        T gpx = o1r[x] * isr, dxx = o1i[x] * isi;
         const bool pml = (x < nh) || (x >= nx - nh);
         const int ai = (x < nh) ? x : x - (nx - nh) + nh;
         if (MODE != 2 && k == a.nz - 1) a.TOPDX[(size_t)b * nx + x] = dxx;
@@ -99,6 +100,8 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
             }
             o1r[x] = vxs;
             o1i[x] = vzs;
+            mr2 = fmax(mr2, fabs(vxs));
+            mi2 = fmax(mi2, fabs(vzs));
         } else if (pml) {
             // closing pass: pmlvarsx += deltat * scrpmlx (step.f90:112-115)
             for (int c = 0; c < 2; c++) {
@@ -108,16 +111,19 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
         }
     }
     if (MODE == 2 || !a.flows) return;
+    T sr2, si2, isr2, isi2;
+    warp_row_scale(mr2, sr2, isr2);
+    warp_row_scale(mi2, si2, isi2);
     __syncwarp();
     T *gr = (o1r == xr) ? yr : xr, *gi = (o1r == xr) ? yi : xi;
     T *o2r, *o2i;
-    fft_deriv<T, N>(o1r, o1i, gr, gi, a.twr, a.twi, a.kap, a.stretchx, lane, o2r, o2i);
+    fft_deriv<T, N>(o1r, o1i, gr, gi, a.twr, a.twi, a.kap, a.stretchx, lane, o2r, o2i, sr2, si2);
     __syncwarp();
     const T *v0xk = a.v0x + (size_t)b * a.bg2 + ro;
     for (int x = lane; x < nx; x += WARP) {
         const T w = T(-2) * a.fsign * __ldg(v0xk + x);
-        a.FXX[(size_t)b * F + ro + x] = w * o2r[x];
-        a.FXZ[(size_t)b * F + ro + x] = w * o2i[x];
+        a.FXX[(size_t)b * F + ro + x] = w * (o2r[x] * isr2);
+        a.FXZ[(size_t)b * F + ro + x] = w * (o2i[x] * isi2);
     }
 }
 
@@ -134,17 +140,23 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) ddx_kernel(const T *__restrict_
     if (r0 >= nrows) return;
     const bool two = r0 + 1 < nrows;
     T *xr = sm + warp * 4 * N, *xi = xr + N, *yr = xi + N, *yi = yr + N;
+    T mr = T(0), mi = T(0);
     for (int x = lane; x < N; x += WARP) {
         xr[x] = var[(size_t)r0 * N + x];
         xi[x] = two ? var[(size_t)(r0 + 1) * N + x] : T(0);
+        mr = fmax(mr, fabs(xr[x]));
+        mi = fmax(mi, fabs(xi[x]));
     }
+    T sr, si, isr, isi;
+    warp_row_scale(mr, sr, isr);
+    warp_row_scale(mi, si, isi);
     __syncwarp();
     T *orr, *oi;
-    fft_deriv<T, N>(xr, xi, yr, yi, twr, twi, kap, stretchx, lane, orr, oi);
+    fft_deriv<T, N>(xr, xi, yr, yi, twr, twi, kap, stretchx, lane, orr, oi, sr, si);
     __syncwarp();
     for (int x = lane; x < N; x += WARP) {
-        dvar[(size_t)r0 * N + x] = orr[x];
-        if (two) dvar[(size_t)(r0 + 1) * N + x] = oi[x];
+        dvar[(size_t)r0 * N + x] = orr[x] * isr;
+        if (two) dvar[(size_t)(r0 + 1) * N + x] = oi[x] * isi;
     }
 }
 
@@ -229,28 +241,42 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) kacc_row_kernel(KAccArgs<T> a)
     const T *f = a.fsn + a.fbase + (size_t)b * a.fstride;
     const T *av = a.adj + (size_t)b * a.astride;
     T *w = a.work + (size_t)b * 4 * F;
+    // forward xi_x with adjoint v_x, then forward v_x with v_z: the forward and adjoint fields
+    // carry unrelated normalisations, so each row is scaled before it shares an FFT
+    T mr = T(0), mi = T(0);
     for (int x = lane; x < N; x += WARP) {
         xr[x] = f[0 * F + ro + x];
         xi[x] = av[ro + x];
+        mr = fmax(mr, fabs(xr[x]));
+        mi = fmax(mi, fabs(xi[x]));
     }
+    T sr, si, isr, isi;
+    warp_row_scale(mr, sr, isr);
+    warp_row_scale(mi, si, isi);
     __syncwarp();
     T *o1r, *o1i;
-    fft_deriv<T, N>(xr, xi, yr, yi, a.twr, a.twi, a.kap, a.stretchx, lane, o1r, o1i);
+    fft_deriv<T, N>(xr, xi, yr, yi, a.twr, a.twi, a.kap, a.stretchx, lane, o1r, o1i, sr, si);
     __syncwarp();
+    T mr2 = T(0), mi2 = T(0);
     for (int x = lane; x < N; x += WARP) {
-        w[0 * F + ro + x] = o1r[x];
-        w[1 * F + ro + x] = o1i[x];
+        w[0 * F + ro + x] = o1r[x] * isr;
+        w[1 * F + ro + x] = o1i[x] * isi;
         o1r[x] = f[2 * F + ro + x];
         o1i[x] = f[3 * F + ro + x];
+        mr2 = fmax(mr2, fabs(o1r[x]));
+        mi2 = fmax(mi2, fabs(o1i[x]));
     }
+    T sr2, si2, isr2, isi2;
+    warp_row_scale(mr2, sr2, isr2);
+    warp_row_scale(mi2, si2, isi2);
     __syncwarp();
     T *gr = (o1r == xr) ? yr : xr, *gi = (o1r == xr) ? yi : xi;
     T *o2r, *o2i;
-    fft_deriv<T, N>(o1r, o1i, gr, gi, a.twr, a.twi, a.kap, a.stretchx, lane, o2r, o2i);
+    fft_deriv<T, N>(o1r, o1i, gr, gi, a.twr, a.twi, a.kap, a.stretchx, lane, o2r, o2i, sr2, si2);
     __syncwarp();
     for (int x = lane; x < N; x += WARP) {
-        w[2 * F + ro + x] = o2r[x];
-        w[3 * F + ro + x] = o2i[x];
+        w[2 * F + ro + x] = o2r[x] * isr2;
+        w[3 * F + ro + x] = o2i[x] * isi2;
     }
 }
 

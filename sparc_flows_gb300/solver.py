@@ -125,7 +125,7 @@ class WaveSolver:
         cfg.steps_out, cfg.k_inj, cfg.k_obs, cfg.src_until = run.steps_out, k_inj, self.o_rad, run.src_until
         cfg.filter_k0, cfg.filter_all_x = run.filter_kst - 1, int(run.filter_all_x)
         cfg.compensated = int(os.environ.get("SPARC_COMPENSATED", "0"))
-        cfg.column_impl = int(os.environ.get("SPARC_COLUMN_IMPL", "1"))
+        cfg.column_impl = int(os.environ.get("SPARC_COLUMN_IMPL", "2"))
         cfg.column_block = int(os.environ.get("SPARC_COLUMN_BLOCK", "32"))
         self.cfg = cfg
         h = ctypes.c_void_p()

@@ -76,3 +76,29 @@ def test_partitioned_tables_other_depths(nz):
     rc = capi.lib().sparc_zsolve_host(nz, 1, 32, b.ctypes.data_as(dp), out.ctypes.data_as(dp), None, 3)
     assert rc == 0
     assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("ibc", [1, 2, 3])
+@pytest.mark.parametrize("nz", [100, 300, 384])
+def test_banded_form_matches_dbyd2(ibc, nz):
+    """The banded inverse used by FP32 column passes: right-hand side as dbyd2 forms it, then a
+    Toeplitz band of T^{-1} plus rank-2 corners; agrees with dbyd2 to 2e-9 of the result."""
+    rng = np.random.default_rng(100 * ibc + nz)
+    n1 = 5
+    z = np.linspace(0.0, 1.0, nz)[:, None]
+    b = np.sin(9.0 * z + rng.uniform(0, 6, n1)) + 0.05 * rng.standard_normal((nz, n1))
+    preset = rng.standard_normal(n1)
+    pre_full = np.zeros((nz, n1))
+    if ibc == 2:
+        pre_full[0] = preset
+    if ibc == 3:
+        pre_full[nz - 1] = preset
+    ref = O.dbyd2(b, ibc, preset=pre_full)
+    out = np.zeros((nz, n1))
+    err = ctypes.c_double()
+    dp = ctypes.POINTER(ctypes.c_double)
+    rc = capi.lib().sparc_zband_host(nz, ibc, b.ctypes.data_as(dp), out.ctypes.data_as(dp),
+                                     preset.ctypes.data_as(dp), n1, ctypes.byref(err))
+    assert rc == 0
+    assert err.value < 1e-9
+    assert np.abs(out - ref).max() <= 2e-9 * np.abs(ref).max()
