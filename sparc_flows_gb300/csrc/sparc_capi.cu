@@ -174,17 +174,17 @@ bool build_ztab(int nz, int ibc, int nch, int L, HostZTab &t)
 }
 
 // ---------------------------------------------------------------------------------------------
-// Banded form of the compact derivative (FP32 column pass).  The right-hand side is formed
-// exactly as dbyd2 forms it; the tridiagonal solve x = T^{-1} rhs becomes a band sum.  Away
-// from the ends T is Toeplitz (1/3, 1, 1/3), whose inverse decays like r^|d|,
-// r = -(3 - sqrt 5)/2 = -0.382, so t[d] = T^{-1}[kc][kc+d] for |d| <= 20 holds the interior
-// rows to 3e-9 of t[0].  The boundary rows of T (dbyd2.f:151-196) and the finite ends leave a
-// correction T^{-1} - band that is confined to the two KC x KC corners (outside them it is below
-// 1e-9) and has rank 2 there; it is factored by cross approximation with full pivoting.
+// Geometric-band form of the compact derivative (FP32 column pass).  The right-hand side is
+// formed exactly as dbyd2 forms it; the tridiagonal solve x = T^{-1} rhs is replaced by the
+// inverse of the infinite Toeplitz operator (1/3, 1, 1/3), whose entries are exactly geometric,
+// t0 r^|d| with r = -(3 - sqrt 5)/2, applied with rhs zero outside 0..nz-1.  The boundary rows
+// of T (dbyd2.f:151-196) and the finite ends make T^{-1} differ from it only near the two
+// corners (elsewhere by < 1e-9 of t0), where the difference has rank 2 on a KC x KC block; it is
+// factored by cross approximation with full pivoting.
 // ---------------------------------------------------------------------------------------------
 struct HostBand {
     int nz = 0, q = 0;
-    double t[BAND_W + 1] = {};
+    double t0 = 0, r = 0;
     std::vector<double> uv;  // Ub [KC][Q], Vb [Q][KC], Ut [KC][Q], Vt [Q][KC]
     double err = 0;          // max |T^{-1} - band - corners| / max |T^{-1}|
 };
@@ -212,8 +212,8 @@ static int cross_approx(std::vector<double> C, int n, int qmax, double tol, doub
 
 bool build_band(const HostZTab &tz, HostBand &h)
 {
-    const int nz = tz.nz, W = BAND_W, KC = BAND_KC, Q = BAND_Q;
-    if (nz < 2 * KC + 2 * W) return false;
+    const int nz = tz.nz, KC = BAND_KC, Q = BAND_Q;
+    if (nz < 2 * KC + 2 * BAND_W) return false;
     h.nz = nz;
     // T^{-1} column by column (diag 1, sub lowr, super uppr), Thomas on unit vectors
     std::vector<double> gam(nz), bet(nz), Ti((size_t)nz * nz, 0.0), y(nz);
@@ -228,8 +228,12 @@ bool build_band(const HostZTab &tz, HostBand &h)
         for (int k = 0; k < nz; k++) Ti[(size_t)k * nz + col] = y[k];
     }
     const int kc = nz / 2;
-    for (int d = 0; d <= W; d++) h.t[d] = Ti[(size_t)kc * nz + kc + d];
-    auto band = [&](int k, int j) { const int d = std::abs(k - j); return d <= W ? h.t[d] : 0.0; };
+    h.t0 = Ti[(size_t)kc * nz + kc];
+    h.r = Ti[(size_t)kc * nz + kc + 1] / h.t0;
+    std::vector<double> rp(nz + 1);
+    rp[0] = 1.0;
+    for (int d = 1; d <= nz; d++) rp[d] = rp[d - 1] * h.r;
+    auto band = [&](int k, int j) { return h.t0 * rp[std::abs(k - j)]; };
     double mx = 0.0;
     for (double v : Ti) mx = std::max(mx, std::fabs(v));
     h.uv.assign((size_t)4 * KC * Q, 0.0);
@@ -271,10 +275,10 @@ static double zrhs_host(const HostZTab &t, const double *b, int n1, int i, int k
     return r;
 }
 
-// Host evaluation of the banded form (same algebra as the device code), unstretched.
+// Host evaluation of the geometric-band form, unstretched: x = t0 sum_d r^|d| rhs[k+d] + corners.
 void zband_host(const HostZTab &t, const HostBand &h, const double *b, double *x, const double *preset_v, int n1)
 {
-    const int nz = h.nz, W = BAND_W, KC = BAND_KC, Q = BAND_Q, o = nz - KC;
+    const int nz = h.nz, KC = BAND_KC, Q = BAND_Q, o = nz - KC;
     const double *Ub = h.uv.data(), *Vb = Ub + KC * Q, *Ut = Vb + KC * Q, *Vt = Ut + KC * Q;
     std::vector<double> rhs(nz);
     for (int i = 0; i < n1; i++) {
@@ -283,9 +287,14 @@ void zband_host(const HostZTab &t, const HostBand &h, const double *b, double *x
         for (int q = 0; q < Q; q++)
             for (int j = 0; j < KC; j++) { sb[q] += Vb[q * KC + j] * rhs[j]; st[q] += Vt[q * KC + j] * rhs[o + j]; }
         for (int k = 0; k < nz; k++) {
-            double v = 0.0;
-            for (int d = -W; d <= W; d++)
-                if (k + d >= 0 && k + d < nz) v += h.t[std::abs(d)] * rhs[k + d];
+            // sum_{d>=1} r^d (rhs[k-d] + rhs[k+d]), accumulated outward from the row
+            double v = rhs[k], L = 0.0, U = 0.0, rd = 1.0;
+            for (int d = 1; d < nz; d++) {
+                rd *= h.r;
+                if (k - d >= 0) L += rd * rhs[k - d];
+                if (k + d < nz) U += rd * rhs[k + d];
+            }
+            v = h.t0 * (v + L + U);
             if (k < KC)
                 for (int q = 0; q < Q; q++) v += Ub[k * Q + q] * sb[q];
             if (k >= o)
@@ -583,8 +592,8 @@ int alloc_solver(sparc_plan *p)
         bool ok = col_band_smem_bytes(nz, R, bcw) <= (size_t)maxsm;
         HostBand hb[3];
         for (int i = 0; i < 3 && ok; i++) ok = build_band(p->hz[i + 1], hb[i]);
-        for (int i = 1; i < 3 && ok; i++)
-            for (int d = 0; d <= BAND_W; d++) ok = ok && std::fabs(hb[i].t[d] - hb[0].t[d]) <= 1e-12 * std::fabs(hb[0].t[0]);
+        for (int i = 1; i < 3 && ok; i++)  // the interior operator does not depend on the boundary condition
+            ok = std::fabs(hb[i].t0 - hb[0].t0) <= 1e-12 * std::fabs(hb[0].t0) && std::fabs(hb[i].r - hb[0].r) <= 1e-12;
         for (int i = 0; i < 3 && ok; i++) {
             std::vector<float> f(hb[i].uv.begin(), hb[i].uv.end());
             void *ptr = nullptr;
@@ -594,7 +603,10 @@ int alloc_solver(sparc_plan *p)
             S.band.uv[i] = (const float *)ptr;
         }
         if (ok) {
-            for (int d = 0; d <= BAND_W; d++) S.band.t[d] = (float)hb[0].t[d];
+            S.band.t0 = (float)hb[0].t0;
+            S.band.r = (float)hb[0].r;
+            double rp = 1.0;
+            for (int d = 0; d < BAND_NPOW; d++) { S.band.rpow[d] = (float)rp; rp *= hb[0].r; }
             S.band_R = R;
             S.band_cw = bcw;
         }

@@ -1,21 +1,26 @@
-// sparc_col_band.cu -- column pass of an RK stage with the banded compact derivative (FP32).
+// sparc_col_band.cu -- column pass of an RK stage with the geometric-band compact derivative
+// (FP32 plans).
 //
 // Same physics as col_stage_kernel (sparc_col.cu, physics2d.f90:943-1094); the tridiagonal
-// solve of every z-derivative (dbyd2.f:8-235, mtridag.f:96-112) is replaced by its banded
-// inverse, which has no serial dependence along z:
-//   1. rhs[k] is formed exactly as dbyd2 forms it (c1/c2 differences, boundary closures, the
-//      caller-set row) and stored in a zero-padded shared-memory column;
-//   2. x[k] = sum_{|d|<=20} t[|d|] rhs[k+d] + rank-2 corner corrections (BandDev).
-// The band truncation is 5e-10 of t[0], far below FP32 rounding; FP64 plans keep the exact
-// partitioned solve.
+// solve of every z-derivative (dbyd2.f:8-235, mtridag.f:96-112) is replaced by
+//   x[k] = t0 (rhs[k] + sum_{d>=1} r^d (rhs[k-d] + rhs[k+d])) + rank-2 corner corrections,
+// the inverse of the infinite Toeplitz operator (1/3, 1, 1/3) (r = -0.382) plus the exact
+// correction near both ends (BandDev).  rhs is formed exactly as dbyd2 forms it.
 //
 // A block owns CW adjacent x-columns (32, 16 or 8) of one solve over the full depth; thread
-// group g (CW threads, one per column) holds rows [g R, g R + R).  A warp therefore reads 32/CW
-// rows that are R apart; with R odd for CW < 32 they fall on disjoint banks, so shared memory
-// is conflict-free.  Narrow blocks let 2 (CW 16) or 4 (CW 8) blocks share an SM, so one block's
-// barrier and load waits overlap another's band sums.  The band coefficients are kernel
-// parameters addressed with compile-time offsets.  Shared memory: two field columns
-// F[nz][CW] and two padded right-hand-side columns [G R + 40][CW].
+// group g (CW threads, one per column) holds rows [g R, g R + R) and keeps their right-hand
+// sides in registers.  The two geometric sums are running sums over the group's own rows,
+//   L[m+1] = r (rhs[m] + L[m]),   U[m-1] = r (rhs[m] + U[m]),
+// stable in both directions (|r| < 1), seeded by carries of the three neighbouring groups on
+// each side (sum_m r^(n-m) rhs[m] and sum_m r^(m+1) rhs[m], exchanged through shared memory;
+// the terms beyond three groups are below r^27 = 5e-12).  Per derivative a thread reads its
+// R + 4 field values and six carries, and does about 15 R flops; there is no serial chain
+// longer than R along z.
+//
+// A warp reads 32/CW rows that are R apart; with R odd for CW < 32 they fall on disjoint banks.
+// Narrow blocks let 2 (CW 16) or 4 (CW 8) blocks share an SM, so one block's barrier and load
+// waits overlap another's arithmetic.  Shared memory: two field columns F[nz][CW], two
+// right-hand-side columns [nz][CW], the carries of two derivatives and seven depth profiles.
 #include "sparc_common.cuh"
 
 namespace sparc {
@@ -24,87 +29,161 @@ template <int CW>
 constexpr int band_maxg() { return CW == 32 ? 32 : 28; }  // thread groups per block
 template <int CW>
 constexpr int band_minb() { return CW == 32 ? 1 : (CW == 16 ? 2 : 4); }  // resident blocks per SM
+template <int R>
+constexpr int band_gb() { return (BAND_KC + R - 1) / R; }  // groups that can touch the bottom corner
+template <int R>
+constexpr int band_gt() { return (BAND_KC + R - 1) / R + 1; }  // ... the top corner
 
-// x[r] = sum_d t[|d|] rhs[k0 + r + d] for r < R (rhs rows outside 0..nz-1 read as zero).
+// Shared carries of one derivative: CL, CU [G][CW], corner partial products PB [GB][Q][CW],
+// PT [GT][Q][CW].
 template <int CW, int R>
-__device__ __forceinline__ void band_sum(const BandDev &bd, const float *Rp, int c, int k0, float (&x)[R])
+struct BandCarry {
+    float *CL, *CU, *PB, *PT;
+    __device__ BandCarry(float *base, int G)
+    {
+        CL = base;
+        CU = CL + G * CW;
+        PB = CU + G * CW;
+        PT = PB + band_gb<R>() * BAND_Q * CW;
+    }
+    static __host__ __device__ constexpr int floats_fixed() { return (band_gb<R>() + band_gt<R>()) * BAND_Q * CW; }
+};
+
+// Right-hand sides of dbyd2 for the rows [k0, k0 + n) of field column Fc (rows beyond n: 0),
+// also stored to the column Rc for band_eval.
+template <int CW, int R>
+__device__ __forceinline__ void band_rhs(const ZTab<float> &tb, const float *Fc, float *Rc, int c, int k0, int n,
+                                         int nz, float preset, float (&rhs)[R])
 {
+    float w[R + 4];  // rows k0-2 .. k0+R+1
 #pragma unroll
-    for (int r = 0; r < R; r++) x[r] = 0.f;
+    for (int i = 0; i < R + 4; i++) {
+        const int k = k0 - 2 + i;
+        w[i] = (k >= 0 && k < nz) ? Fc[k * CW + c] : 0.f;
+    }
 #pragma unroll
-    for (int i = -BAND_W; i < R + BAND_W; i++) {
-        const float v = Rp[(k0 + i) * CW + c];
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int d = i - r;
-            if (d >= -BAND_W && d <= BAND_W) x[r] = fmaf(bd.t[d < 0 ? -d : d], v, x[r]);
+    for (int m = 0; m < R; m++) {
+        const int k = k0 + m;
+        float v = 0.f;
+        if (m < n) {
+            if (k >= 2 && k <= nz - 3)
+                v = tb.c1 * (w[m + 3] - w[m + 1]) + tb.c2 * (w[m + 4] - w[m]);
+            else
+                v = zrhs(tb, Fc, CW, c, k, nz, preset);  // boundary closures, caller-set row
+            Rc[k * CW + c] = v;
         }
+        rhs[m] = v;
     }
 }
 
-// Corner corrections of the rows [k0, k0 + n) that lie within BAND_KC of either end.
+// Carries of the group's right-hand sides and its partial products with the corner factors.
 template <int CW, int R>
-__device__ __forceinline__ void band_corners(const float *__restrict__ uv, const float *Rp, int c, int k0, int n,
-                                             int nz, float (&x)[R])
+__device__ __forceinline__ void band_publish(const BandDev &bd, const float *__restrict__ uv, const BandCarry<CW, R> &cb,
+                                             int c, int g, int k0, int n, int nz, const float (&rhs)[R])
 {
     constexpr int KC = BAND_KC, Q = BAND_Q;
-    if (k0 < KC) {
-        const float *Ub = uv, *Vb = uv + KC * Q;
-        float s[Q];
-#pragma unroll
-        for (int q = 0; q < Q; q++) s[q] = 0.f;
-#pragma unroll 4
-        for (int j = 0; j < KC; j++) {
-            const float v = Rp[j * CW + c];
-#pragma unroll
-            for (int q = 0; q < Q; q++) s[q] = fmaf(__ldg(Vb + q * KC + j), v, s[q]);
-        }
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int k = k0 + r;
-            if (r < n && k < KC)
-#pragma unroll
-                for (int q = 0; q < Q; q++) x[r] = fmaf(__ldg(Ub + k * Q + q), s[q], x[r]);
-        }
-    }
-    const int o = nz - KC;
-    if (k0 + n > o) {
-        const float *Ut = uv + 2 * KC * Q, *Vt = uv + 3 * KC * Q;
-        float s[Q];
-#pragma unroll
-        for (int q = 0; q < Q; q++) s[q] = 0.f;
-#pragma unroll 4
-        for (int j = 0; j < KC; j++) {
-            const float v = Rp[(o + j) * CW + c];
-#pragma unroll
-            for (int q = 0; q < Q; q++) s[q] = fmaf(__ldg(Vt + q * KC + j), v, s[q]);
-        }
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int k = k0 + r - o;
-            if (r < n && k >= 0)
-#pragma unroll
-                for (int q = 0; q < Q; q++) x[r] = fmaf(__ldg(Ut + k * Q + q), s[q], x[r]);
-        }
-    }
-}
-
-// Right-hand side of the rows [k0, k0 + n) of field column Fc into the padded column Rp.
-template <int CW, int R>
-__device__ __forceinline__ void band_rhs(const ZTab<float> &tb, const float *Fc, float *Rp, int c, int k0, int n,
-                                         int nz, float preset)
-{
+    const float r = bd.r;
+    float cl = 0.f, cu = 0.f;
 #pragma unroll
     for (int m = 0; m < R; m++)
-        if (m < n) Rp[(k0 + m) * CW + c] = zrhs(tb, Fc, CW, c, k0 + m, nz, preset);
+        if (m < n) cl = r * (cl + rhs[m]);
+#pragma unroll
+    for (int m = R - 1; m >= 0; m--)
+        if (m < n) cu = r * (cu + rhs[m]);
+    cb.CL[g * CW + c] = cl;
+    cb.CU[g * CW + c] = cu;
+    if (k0 < KC) {
+        const float *Vb = uv + KC * Q;
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            float p = 0.f;
+#pragma unroll
+            for (int m = 0; m < R; m++)
+                if (m < n && k0 + m < KC) p = fmaf(__ldg(Vb + q * KC + k0 + m), rhs[m], p);
+            cb.PB[(g * Q + q) * CW + c] = p;
+        }
+    }
+    const int o = nz - KC, gt0 = o / R;
+    if (g >= gt0) {
+        const float *Vt = uv + 3 * KC * Q;
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            float p = 0.f;
+#pragma unroll
+            for (int m = 0; m < R; m++)
+                if (m < n && k0 + m >= o) p = fmaf(__ldg(Vt + q * KC + (k0 + m - o)), rhs[m], p);
+            cb.PT[((g - gt0) * Q + q) * CW + c] = p;
+        }
+    }
 }
 
+// x[m] = (T^{-1} rhs)[k0 + m] for m < n, from the group's own right-hand sides (column Rc) and
+// the carries.
 template <int CW, int R>
-__device__ __forceinline__ void band_deriv(const BandDev &bd, int which, const float *Rp, int c, int k0, int n,
-                                           int nz, float (&x)[R])
+__device__ __forceinline__ void band_eval(const BandDev &bd, const float *__restrict__ uv, const BandCarry<CW, R> &cb,
+                                          int c, int g, int G, int k0, int n, int nz, const float *Rc, float (&x)[R])
 {
-    band_sum<CW, R>(bd, Rp, c, k0, x);
-    band_corners<CW, R>(bd.uv[which], Rp, c, k0, n, nz, x);
+    constexpr int KC = BAND_KC, Q = BAND_Q;
+    float rhs[R];
+#pragma unroll
+    for (int m = 0; m < R; m++) rhs[m] = (m < n) ? Rc[(k0 + m) * CW + c] : 0.f;
+    const float r = bd.r, rR = bd.rpow[R], r2R = bd.rpow[2 * R];
+    float l = 0.f, u = 0.f;  // sum_{d>=1} r^d rhs below the first row / above the last row
+    if (g >= 1) l = cb.CL[(g - 1) * CW + c];
+    if (g >= 2) l = fmaf(rR, cb.CL[(g - 2) * CW + c], l);
+    if (g >= 3) l = fmaf(r2R, cb.CL[(g - 3) * CW + c], l);
+    if (g + 1 < G) u = cb.CU[(g + 1) * CW + c];
+    if (g + 2 < G) u = fmaf(rR, cb.CU[(g + 2) * CW + c], u);
+    if (g + 3 < G) u = fmaf(r2R, cb.CU[(g + 3) * CW + c], u);
+#pragma unroll
+    for (int m = R - 1; m >= 0; m--) {
+        if (m < n) {
+            x[m] = rhs[m] + u;
+            u = r * (rhs[m] + u);
+        } else {
+            x[m] = 0.f;
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < R; m++) {
+        x[m] = bd.t0 * (x[m] + l);
+        l = r * (rhs[m] + l);
+    }
+    if (k0 < KC) {
+        float s[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            s[q] = 0.f;
+#pragma unroll
+            for (int gg = 0; gg < band_gb<R>(); gg++)
+                if (gg * R < KC) s[q] += cb.PB[(gg * Q + q) * CW + c];
+        }
+        const float *Ub = uv;
+#pragma unroll
+        for (int m = 0; m < R; m++) {
+            const int k = k0 + m;
+            if (m < n && k < KC)
+#pragma unroll
+                for (int q = 0; q < Q; q++) x[m] = fmaf(__ldg(Ub + k * Q + q), s[q], x[m]);
+        }
+    }
+    const int o = nz - KC, gt0 = o / R;
+    if (k0 + n > o) {
+        float s[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            s[q] = 0.f;
+            for (int gg = gt0; gg < G; gg++) s[q] += cb.PT[((gg - gt0) * Q + q) * CW + c];
+        }
+        const float *Ut = uv + 2 * KC * Q;
+#pragma unroll
+        for (int m = 0; m < R; m++) {
+            const int k = k0 + m - o;
+            if (m < n && k >= 0)
+#pragma unroll
+                for (int q = 0; q < Q; q++) x[m] = fmaf(__ldg(Ut + k * Q + q), s[q], x[m]);
+        }
+    }
 }
 
 template <int CW, int R>
@@ -113,11 +192,25 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     extern __shared__ __align__(16) float smb[];
     const int nz = a.nz, nx = a.nx;
     const int G = blockDim.x / CW;
-    const int NPR = G * R + 2 * BAND_W;
+    const int ncar = 2 * G * CW + BandCarry<CW, R>::floats_fixed();
     float *FA = smb;
     float *FB = FA + (size_t)nz * CW;
-    float *RA = FB + (size_t)nz * CW + BAND_W * CW;  // row 0 of a padded column
-    float *RB = RA + (size_t)NPR * CW;
+    float *RA = FB + (size_t)nz * CW;  // right-hand sides
+    float *RB = RA + (size_t)nz * CW;
+    const BandCarry<CW, R> C0(RB + (size_t)nz * CW, G), C1(RB + (size_t)nz * CW + ncar, G);
+    // depth profiles: stretch, rhoinv, rho0, gradp0_z, gradrho0_z, g, c2rho0 (1-D case)
+    float *KP = RB + (size_t)nz * CW + 2 * ncar;
+    float *Kst = KP, *Kri = KP + nz, *Kr0 = KP + 2 * nz, *Kgp = KP + 3 * nz, *Kgr = KP + 4 * nz, *Kg = KP + 5 * nz,
+          *Kc2 = KP + 6 * nz;
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+        Kst[k] = Kst[k];
+        Kri[k] = Kri[k];
+        Kr0[k] = Kr0[k];
+        Kgp[k] = Kgp[k];
+        Kgr[k] = Kgr[k];
+        Kg[k] = Kg[k];
+        Kc2[k] = a.c2d ? 0.f : Kc2[k];
+    }
     const int c = threadIdx.x % CW, g = threadIdx.x / CW;
     const int x = blockIdx.x * CW + c;
     const int b = blockIdx.y;
@@ -129,20 +222,11 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     const float bs = a.bs, bsm1 = a.bsm1;
     const int time = *a.d_time;
 
-    // zero rows [-W, 0) and [nz, G R + W) of both right-hand-side columns
-    {
-        const int npad = BAND_W + (G * R + BAND_W - nz);
-        for (int i = threadIdx.x; i < npad * CW; i += blockDim.x) {
-            const int rr = i / CW, cc = i % CW;
-            const int k = rr < BAND_W ? rr - BAND_W : nz + (rr - BAND_W);
-            RA[k * CW + cc] = 0.f;
-            RB[k * CW + cc] = 0.f;
-        }
-    }
     // ---- 1: xi_z at stage s (scr xi_z = v_z of stage s-1 with the RHS boundary zeros)
     float xz[R];
 #pragma unroll
     for (int m = 0; m < R; m++) {
+        xz[m] = 0.f;
         if (m < n) {
             const int k = k0 + m;
             const size_t q = (size_t)k * nx + x;
@@ -159,19 +243,23 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     }
     __syncthreads();
     // ---- 2: right-hand side of d xi_z/dz (ibc 3, top value -dxi_x/dx * unstretch)
-    const float preset3 = -__ldg(a.TOPDX + (size_t)b * nx + x) * a.unstretch_top;
-    band_rhs<CW, R>(a.z3, FA, RA, c, k0, n, nz, preset3);
+    {
+        float ra[R];
+        const float preset3 = -__ldg(a.TOPDX + (size_t)b * nx + x) * a.unstretch_top;
+        band_rhs<CW, R>(a.z3, FA, RA, c, k0, n, nz, preset3, ra);
+        band_publish<CW, R>(bd, bd.uv[2], C0, c, g, k0, n, nz, ra);
+    }
     __syncthreads();
     // ---- 3: d xi_z/dz, vertical PML, divergence, pressure; v_x of stage s
     {
         float d[R];
-        band_deriv<CW, R>(bd, 2, RA, c, k0, n, nz, d);
+        band_eval<CW, R>(bd, bd.uv[2], C0, c, g, G, k0, n, nz, RA, d);
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
                 const int k = k0 + m;
                 const size_t q = (size_t)k * nx + x;
-                float dzz = d[m] * __ldg(a.stretch + k);
+                float dzz = d[m] * Kst[k];
                 const int pi = pml_row(a, k);
                 float fd = 1.f;
                 if (pi >= 0) {
@@ -185,11 +273,11 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
                     fd = __ldg(a.fdz + qb);
                 }
                 const float div = __ldg(a.DX + (size_t)b * F + q) + dzz;
-                const float c2r = a.c2d ? __ldg(a.c2rho0 + (size_t)b * a.bg2 + q) : __ldg(a.c2rho0 + k);
-                const float gp = __ldg(a.gp0 + k) * fd, gr = __ldg(a.gr0 + k) * fd;
+                const float c2r = a.c2d ? __ldg(a.c2rho0 + (size_t)b * a.bg2 + q) : Kc2[k];
+                const float gp = Kgp[k] * fd, gr = Kgr[k] * fd;
                 const float p = -c2r * div - gp * xz[m];
-                const float rho = -__ldg(a.rho0 + k) * div - gr * xz[m];
-                xz[m] = rho * __ldg(a.g + k);
+                const float rho = -Kr0[k] * div - gr * xz[m];
+                xz[m] = rho * Kg[k];
                 FA[k * CW + c] = p;
                 a.P[(size_t)b * F + q] = p;
                 float vx = __ldg(Ab + F_VX * F + q);
@@ -200,18 +288,26 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     }
     __syncthreads();
     // ---- 4: right-hand sides of dp/dz (ibc 2, bottom value 0) and dv_x/dz (ibc 1)
-    band_rhs<CW, R>(a.z2, FA, RA, c, k0, n, nz, 0.f);
-    if (a.flows) band_rhs<CW, R>(a.z1, FB, RB, c, k0, n, nz, 0.f);
+    {
+        float rr[R];
+        band_rhs<CW, R>(a.z2, FA, RA, c, k0, n, nz, 0.f, rr);
+        band_publish<CW, R>(bd, bd.uv[1], C0, c, g, k0, n, nz, rr);
+    }
+    if (a.flows) {
+        float rr[R];
+        band_rhs<CW, R>(a.z1, FB, RB, c, k0, n, nz, 0.f, rr);
+        band_publish<CW, R>(bd, bd.uv[0], C1, c, g, k0, n, nz, rr);
+    }
     __syncthreads();
     // ---- 5: gradient of p, RHS v_z without advection; advection of v_x along z; v_z of stage s
     {
         float d[R];
-        band_deriv<CW, R>(bd, 1, RA, c, k0, n, nz, d);
+        band_eval<CW, R>(bd, bd.uv[1], C0, c, g, G, k0, n, nz, RA, d);
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
                 const int k = k0 + m;
-                float gpz = d[m] * __ldg(a.stretch + k);
+                float gpz = d[m] * Kst[k];
                 const int pi = pml_row(a, k);
                 if (pi >= 0) {
                     const size_t qz = (((size_t)b * 2 + 1) * a.nzpml + pi) * nx + x;  // psi_p
@@ -222,10 +318,10 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
                         __ldg(a.az + qb) * gpz + __ldg(a.bz + qb) * ps;
                     gpz += ps;
                 }
-                xz[m] = -__ldg(a.rhoinv + k) * (gpz + xz[m]);
+                xz[m] = -Kri[k] * (gpz + xz[m]);
             }
         }
-        if (a.flows) band_deriv<CW, R>(bd, 0, RB, c, k0, n, nz, d);
+        if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C1, c, g, G, k0, n, nz, RB, d);
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
@@ -233,7 +329,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
                 const size_t q = (size_t)k * nx + x;
                 float rv = 0.f;
                 if (a.flows) {
-                    const float dvxdz = d[m] * __ldg(a.stretch + k);
+                    const float dvxdz = d[m] * Kst[k];
                     rv = __ldg(a.FXX + (size_t)b * F + q) -
                          2.f * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvxdz;
                 }
@@ -247,12 +343,14 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     __syncthreads();
     // ---- 6: right-hand side of dv_z/dz (ibc 1)
     if (a.flows) {
-        band_rhs<CW, R>(a.z1, FA, RA, c, k0, n, nz, 0.f);
+        float rr[R];
+        band_rhs<CW, R>(a.z1, FA, RA, c, k0, n, nz, 0.f, rr);
+        band_publish<CW, R>(bd, bd.uv[0], C0, c, g, k0, n, nz, rr);
         __syncthreads();
     }
     // ---- 7: finish RHS v_z (advection, source, boundary zeros)
     float d[R];
-    if (a.flows) band_deriv<CW, R>(bd, 0, RA, c, k0, n, nz, d);
+    if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C0, c, g, G, k0, n, nz, RA, d);
     float forcing = 0.f;
     const bool inject = (time <= a.src_until) && (time >= 0) && (time < a.ntab);
     if (inject && a.k_inj >= k0 && a.k_inj < k0 + n) {
@@ -275,7 +373,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
             float r = xz[m];
             if (k == a.k_inj) r += forcing;
             if (a.flows) {
-                const float dvzdz = d[m] * __ldg(a.stretch + k);
+                const float dvzdz = d[m] * Kst[k];
                 r += __ldg(a.FXZ + (size_t)b * F + q) - 2.f * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvzdz;
             }
             if (k == 0 || x == 0 || x == nx - 1) r = 0.f;
@@ -297,18 +395,36 @@ int col_band_rows(int nz, int cw)
     return 0;
 }
 
-size_t col_band_smem_bytes(int nz, int R, int cw)
+template <int CW, int R>
+static size_t band_smem(int nz)
 {
     const int G = (nz + R - 1) / R;
-    return ((size_t)2 * nz + 2 * ((size_t)G * R + 2 * BAND_W)) * cw * sizeof(float);
+    return ((size_t)4 * nz * CW + 2 * ((size_t)2 * G * CW + BandCarry<CW, R>::floats_fixed()) + (size_t)7 * nz) *
+           sizeof(float);
+}
+
+size_t col_band_smem_bytes(int nz, int R, int cw)
+{
+    switch (cw * 100 + R) {
+        case 3208: return band_smem<32, 8>(nz);
+        case 3210: return band_smem<32, 10>(nz);
+        case 3212: return band_smem<32, 12>(nz);
+        case 1609: return band_smem<16, 9>(nz);
+        case 1611: return band_smem<16, 11>(nz);
+        case 1613: return band_smem<16, 13>(nz);
+        case 809: return band_smem<8, 9>(nz);
+        case 811: return band_smem<8, 11>(nz);
+        case 813: return band_smem<8, 13>(nz);
+        default: return ~(size_t)0;
+    }
 }
 
 template <int CW, int R>
 cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st)
 {
     const int G = (a.nz + R - 1) / R;
-    if (G > band_maxg<CW>() || a.nx % CW != 0) return cudaErrorInvalidValue;
-    const size_t smem = col_band_smem_bytes(a.nz, R, CW);
+    if (G > band_maxg<CW>() || a.nx % CW != 0 || R * G - a.nz >= R) return cudaErrorInvalidValue;
+    const size_t smem = band_smem<CW, R>(a.nz);
     cudaError_t e =
         cudaFuncSetAttribute(col_band_kernel<CW, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

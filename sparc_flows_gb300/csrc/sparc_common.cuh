@@ -16,9 +16,10 @@ namespace sparc {
 constexpr int WARP = 32;
 constexpr int MAX_NCH = 24;  // chunks per column (nz <= MAX_NCH * LMAX)
 constexpr int SPARC_DEV_ERR_TMA_TIMEOUT = 1;  // device error flag: a bounded mbarrier wait gave up
-// Banded form of the compact z-derivative (FP32 column pass): T^{-1} as a symmetric Toeplitz
-// band of half-width BAND_W plus rank-BAND_Q corrections on the BAND_KC x BAND_KC corners.
-constexpr int BAND_W = 20, BAND_KC = 24, BAND_Q = 3;
+// Geometric-band form of the compact z-derivative (FP32 column pass): T^{-1} as the inverse of
+// the infinite Toeplitz operator, t0 r^|d|, plus rank-BAND_Q corrections on BAND_KC x BAND_KC
+// corners.  BAND_W: minimum rows of zero padding / depth margin the host checks for.
+constexpr int BAND_W = 20, BAND_KC = 24, BAND_Q = 3, BAND_NPOW = 48;
 
 // Field order of the live state (xi_y and v_y vanish identically in 2-D).
 enum { F_XIX = 0, F_XIZ = 1, F_VX = 2, F_VZ = 3 };
@@ -88,13 +89,15 @@ __device__ __forceinline__ int pml_row(const StepArgs<T> &a, int k)
     return -1;
 }
 
-// Banded compact-derivative tables (FP32 plans).  x = T^{-1} rhs is evaluated as
-//   x[k] = sum_{|d| <= BAND_W} t[|d|] rhs[k+d]        (rhs zero outside 0..nz-1)
-//        + sum_q Ub[k][q] (Vb[q] . rhs[0..KC))         for k < KC
-//        + sum_q Ut[k'][q] (Vt[q] . rhs[nz-KC..nz))    for k' = k - (nz-KC) >= 0
-// uv[i] (boundary condition i+1) holds Ub [KC][Q], Vb [Q][KC], Ut [KC][Q], Vt [Q][KC].
+// Geometric-band tables (FP32 plans).  x = T^{-1} rhs is evaluated as
+//   x[k] = t0 (rhs[k] + sum_{d>=1} r^d (rhs[k-d] + rhs[k+d]))      (rhs zero outside 0..nz-1)
+//        + sum_q Ub[k][q] (Vb[q] . rhs[0..KC))                      for k < KC
+//        + sum_q Ut[k'][q] (Vt[q] . rhs[nz-KC..nz))                 for k' = k - (nz-KC) >= 0
+// uv[i] (boundary condition i+1) holds Ub [KC][Q], Vb [Q][KC], Ut [KC][Q], Vt [Q][KC];
+// rpow[n] = r^n.
 struct BandDev {
-    float t[BAND_W + 1];
+    float t0, r;
+    float rpow[BAND_NPOW];
     const float *uv[3];
 };
 
