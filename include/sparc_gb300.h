@@ -59,8 +59,9 @@ typedef struct {
                                   partitioned solve (other values: 32), 32, 16 or 8 for the banded
                                   pass (other values: 16) */
     int column_impl;           /* column pass: 0 partitioned solve with direct loads, 1 partitioned
-                                  solve with TMA-staged tiles, 2 (FP32 plans) banded inverse of the
-                                  compact operator, FP64 plans then use 0 */
+                                  solve with TMA-staged tiles, 2 (FP32 plans) geometric-band
+                                  inverse of the compact operator with direct loads, 3 (FP32 plans)
+                                  geometric band with TMA-staged tiles; FP64 plans use 0 for 2, 3 */
 } sparc_config_t;
 
 /* Background, all DEVICE pointers to FP64 arrays; copied (and rounded for FP32 plans) into

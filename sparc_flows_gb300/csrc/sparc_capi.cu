@@ -471,6 +471,7 @@ struct Solver {
     BandDev band{};    // banded z-derivative tables (FP32 plans, column_impl 2)
     int band_R = 0;    // rows per thread group of the banded column pass (0: not used)
     int band_cw = 0;   // its block width (columns)
+    int band_tma_R = 0;  // rows per thread group of the TMA-staged banded pass (0: not used)
     std::vector<void *> allocs;
     size_t F = 0;
     T *work = nullptr;  // kernel-accumulation scratch [nb][8][nz][nx]
@@ -584,7 +585,7 @@ int alloc_solver(sparc_plan *p)
     // banded column pass (FP32 only: its truncation at 5e-10 is below FP32 rounding, not FP64's)
     S.band_R = 0;
     const int bcw = (c.column_block == 8 || c.column_block == 16 || c.column_block == 32) ? c.column_block : 16;
-    if (sizeof(T) == 4 && c.column_impl == 2 && nx % bcw == 0 && col_band_rows(nz, bcw) > 0) {
+    if (sizeof(T) == 4 && (c.column_impl == 2 || c.column_impl == 3) && nx % bcw == 0 && col_band_rows(nz, bcw) > 0) {
         const int R = col_band_rows(nz, bcw);
         int maxsm = 0, dev = 0;
         cudaGetDevice(&dev);
@@ -631,6 +632,13 @@ int alloc_solver(sparc_plan *p)
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
             if (smem > (size_t)maxsm) S.have_maps = false;
+            // TMA-staged banded pass (FP32): also the 2-D background tiles it stages
+            const int Rt = col_band_tma_rows(nz);
+            if (sizeof(T) == 4 && c.column_impl == 3 && S.band_R > 0 && Rt > 0 &&
+                col_band_tma_smem_bytes(nz, Rt, boxr) <= (size_t)maxsm &&
+                (!c.c2d || encode_map(&S.maps.C2R, c2rho0, nx, (long long)nbg * nz, boxr, es)) &&
+                (!c.flows || encode_map(&S.maps.V0Z, v0z, nx, (long long)nbg * nz, boxr, es)))
+                S.band_tma_R = Rt;
         }
     }
     return SPARC_OK;
@@ -648,6 +656,12 @@ cudaError_t col_stage(sparc_plan *p, const StepArgs<T> &a, cudaStream_t st)
 {
     Solver<T> &S = solver<T>(p);
     if constexpr (sizeof(T) == 4) {
+        switch (S.band_tma_R) {
+            case 9: return launch_col_stage_band_tma<9>(S.maps, a, S.band, st);
+            case 11: return launch_col_stage_band_tma<11>(S.maps, a, S.band, st);
+            case 13: return launch_col_stage_band_tma<13>(S.maps, a, S.band, st);
+            default: break;
+        }
         switch (S.band_cw * 100 + S.band_R) {
             case 3208: return launch_col_stage_band<32, 8>(a, S.band, st);
             case 3210: return launch_col_stage_band<32, 10>(a, S.band, st);
@@ -817,6 +831,8 @@ int set_background(sparc_plan *p, const sparc_background_t *bg, cudaStream_t st)
     CK(cudaStreamSynchronize(st));
     p->unstretch_top = ut;
     p->have_bg = true;
+    // unstretch_top is a launch argument: a captured graph holds a stale copy
+    if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
     return SPARC_OK;
 }
 

@@ -1,190 +1,15 @@
 // sparc_col_band.cu -- column pass of an RK stage with the geometric-band compact derivative
-// (FP32 plans).
+// (FP32 plans), direct global loads.
 //
-// Same physics as col_stage_kernel (sparc_col.cu, physics2d.f90:943-1094); the tridiagonal
-// solve of every z-derivative (dbyd2.f:8-235, mtridag.f:96-112) is replaced by
-//   x[k] = t0 (rhs[k] + sum_{d>=1} r^d (rhs[k-d] + rhs[k+d])) + rank-2 corner corrections,
-// the inverse of the infinite Toeplitz operator (1/3, 1, 1/3) (r = -0.382) plus the exact
-// correction near both ends (BandDev).  rhs is formed exactly as dbyd2 forms it.
-//
-// A block owns CW adjacent x-columns (32, 16 or 8) of one solve over the full depth; thread
-// group g (CW threads, one per column) holds rows [g R, g R + R) and keeps their right-hand
-// sides in registers.  The two geometric sums are running sums over the group's own rows,
-//   L[m+1] = r (rhs[m] + L[m]),   U[m-1] = r (rhs[m] + U[m]),
-// stable in both directions (|r| < 1), seeded by carries of the three neighbouring groups on
-// each side (sum_m r^(n-m) rhs[m] and sum_m r^(m+1) rhs[m], exchanged through shared memory;
-// the terms beyond three groups are below r^27 = 5e-12).  Per derivative a thread reads its
-// R + 4 field values and six carries, and does about 15 R flops; there is no serial chain
-// longer than R along z.
-//
-// A warp reads 32/CW rows that are R apart; with R odd for CW < 32 they fall on disjoint banks.
-// Narrow blocks let 2 (CW 16) or 4 (CW 8) blocks share an SM, so one block's barrier and load
-// waits overlap another's arithmetic.  Shared memory: two field columns F[nz][CW], two
-// right-hand-side columns [nz][CW], the carries of two derivatives and seven depth profiles.
-#include "sparc_common.cuh"
+// Same physics as col_stage_kernel (sparc_col.cu, physics2d.f90:943-1094); every z-derivative
+// is evaluated by the geometric band of sparc_band.cuh instead of a tridiagonal solve.  A block
+// owns CW adjacent x-columns (32, 16 or 8) of one solve over the full depth.  A warp reads 32/CW
+// rows that are R apart; with R odd for CW < 32 they fall on disjoint banks.  Shared memory:
+// two field columns F[nz][CW], two right-hand-side columns [nz][CW], the carries of two
+// derivatives and seven depth profiles.
+#include "sparc_band.cuh"
 
 namespace sparc {
-
-template <int CW>
-constexpr int band_maxg() { return CW == 32 ? 32 : 28; }  // thread groups per block
-template <int CW>
-constexpr int band_minb() { return CW == 32 ? 1 : (CW == 16 ? 2 : 4); }  // resident blocks per SM
-template <int R>
-constexpr int band_gb() { return (BAND_KC + R - 1) / R; }  // groups that can touch the bottom corner
-template <int R>
-constexpr int band_gt() { return (BAND_KC + R - 1) / R + 1; }  // ... the top corner
-
-// Shared carries of one derivative: CL, CU [G][CW], corner partial products PB [GB][Q][CW],
-// PT [GT][Q][CW].
-template <int CW, int R>
-struct BandCarry {
-    float *CL, *CU, *PB, *PT;
-    __device__ BandCarry(float *base, int G)
-    {
-        CL = base;
-        CU = CL + G * CW;
-        PB = CU + G * CW;
-        PT = PB + band_gb<R>() * BAND_Q * CW;
-    }
-    static __host__ __device__ constexpr int floats_fixed() { return (band_gb<R>() + band_gt<R>()) * BAND_Q * CW; }
-};
-
-// Right-hand sides of dbyd2 for the rows [k0, k0 + n) of field column Fc (rows beyond n: 0),
-// also stored to the column Rc for band_eval.
-template <int CW, int R>
-__device__ __forceinline__ void band_rhs(const ZTab<float> &tb, const float *Fc, float *Rc, int c, int k0, int n,
-                                         int nz, float preset, float (&rhs)[R])
-{
-    float w[R + 4];  // rows k0-2 .. k0+R+1
-#pragma unroll
-    for (int i = 0; i < R + 4; i++) {
-        const int k = k0 - 2 + i;
-        w[i] = (k >= 0 && k < nz) ? Fc[k * CW + c] : 0.f;
-    }
-#pragma unroll
-    for (int m = 0; m < R; m++) {
-        const int k = k0 + m;
-        float v = 0.f;
-        if (m < n) {
-            if (k >= 2 && k <= nz - 3)
-                v = tb.c1 * (w[m + 3] - w[m + 1]) + tb.c2 * (w[m + 4] - w[m]);
-            else
-                v = zrhs(tb, Fc, CW, c, k, nz, preset);  // boundary closures, caller-set row
-            Rc[k * CW + c] = v;
-        }
-        rhs[m] = v;
-    }
-}
-
-// Carries of the group's right-hand sides and its partial products with the corner factors.
-template <int CW, int R>
-__device__ __forceinline__ void band_publish(const BandDev &bd, const float *__restrict__ uv, const BandCarry<CW, R> &cb,
-                                             int c, int g, int k0, int n, int nz, const float (&rhs)[R])
-{
-    constexpr int KC = BAND_KC, Q = BAND_Q;
-    const float r = bd.r;
-    float cl = 0.f, cu = 0.f;
-#pragma unroll
-    for (int m = 0; m < R; m++)
-        if (m < n) cl = r * (cl + rhs[m]);
-#pragma unroll
-    for (int m = R - 1; m >= 0; m--)
-        if (m < n) cu = r * (cu + rhs[m]);
-    cb.CL[g * CW + c] = cl;
-    cb.CU[g * CW + c] = cu;
-    if (k0 < KC) {
-        const float *Vb = uv + KC * Q;
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            float p = 0.f;
-#pragma unroll
-            for (int m = 0; m < R; m++)
-                if (m < n && k0 + m < KC) p = fmaf(__ldg(Vb + q * KC + k0 + m), rhs[m], p);
-            cb.PB[(g * Q + q) * CW + c] = p;
-        }
-    }
-    const int o = nz - KC, gt0 = o / R;
-    if (g >= gt0) {
-        const float *Vt = uv + 3 * KC * Q;
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            float p = 0.f;
-#pragma unroll
-            for (int m = 0; m < R; m++)
-                if (m < n && k0 + m >= o) p = fmaf(__ldg(Vt + q * KC + (k0 + m - o)), rhs[m], p);
-            cb.PT[((g - gt0) * Q + q) * CW + c] = p;
-        }
-    }
-}
-
-// x[m] = (T^{-1} rhs)[k0 + m] for m < n, from the group's own right-hand sides (column Rc) and
-// the carries.
-template <int CW, int R>
-__device__ __forceinline__ void band_eval(const BandDev &bd, const float *__restrict__ uv, const BandCarry<CW, R> &cb,
-                                          int c, int g, int G, int k0, int n, int nz, const float *Rc, float (&x)[R])
-{
-    constexpr int KC = BAND_KC, Q = BAND_Q;
-    float rhs[R];
-#pragma unroll
-    for (int m = 0; m < R; m++) rhs[m] = (m < n) ? Rc[(k0 + m) * CW + c] : 0.f;
-    const float r = bd.r, rR = bd.rpow[R], r2R = bd.rpow[2 * R];
-    float l = 0.f, u = 0.f;  // sum_{d>=1} r^d rhs below the first row / above the last row
-    if (g >= 1) l = cb.CL[(g - 1) * CW + c];
-    if (g >= 2) l = fmaf(rR, cb.CL[(g - 2) * CW + c], l);
-    if (g >= 3) l = fmaf(r2R, cb.CL[(g - 3) * CW + c], l);
-    if (g + 1 < G) u = cb.CU[(g + 1) * CW + c];
-    if (g + 2 < G) u = fmaf(rR, cb.CU[(g + 2) * CW + c], u);
-    if (g + 3 < G) u = fmaf(r2R, cb.CU[(g + 3) * CW + c], u);
-#pragma unroll
-    for (int m = R - 1; m >= 0; m--) {
-        if (m < n) {
-            x[m] = rhs[m] + u;
-            u = r * (rhs[m] + u);
-        } else {
-            x[m] = 0.f;
-        }
-    }
-#pragma unroll
-    for (int m = 0; m < R; m++) {
-        x[m] = bd.t0 * (x[m] + l);
-        l = r * (rhs[m] + l);
-    }
-    if (k0 < KC) {
-        float s[Q];
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            s[q] = 0.f;
-#pragma unroll
-            for (int gg = 0; gg < band_gb<R>(); gg++)
-                if (gg * R < KC) s[q] += cb.PB[(gg * Q + q) * CW + c];
-        }
-        const float *Ub = uv;
-#pragma unroll
-        for (int m = 0; m < R; m++) {
-            const int k = k0 + m;
-            if (m < n && k < KC)
-#pragma unroll
-                for (int q = 0; q < Q; q++) x[m] = fmaf(__ldg(Ub + k * Q + q), s[q], x[m]);
-        }
-    }
-    const int o = nz - KC, gt0 = o / R;
-    if (k0 + n > o) {
-        float s[Q];
-#pragma unroll
-        for (int q = 0; q < Q; q++) {
-            s[q] = 0.f;
-            for (int gg = gt0; gg < G; gg++) s[q] += cb.PT[((gg - gt0) * Q + q) * CW + c];
-        }
-        const float *Ut = uv + 2 * KC * Q;
-#pragma unroll
-        for (int m = 0; m < R; m++) {
-            const int k = k0 + m - o;
-            if (m < n && k >= 0)
-#pragma unroll
-                for (int q = 0; q < Q; q++) x[m] = fmaf(__ldg(Ut + k * Q + q), s[q], x[m]);
-        }
-    }
-}
 
 template <int CW, int R>
 __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band_kernel(StepArgs<float> a, BandDev bd)
@@ -198,18 +23,17 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     float *RA = FB + (size_t)nz * CW;  // right-hand sides
     float *RB = RA + (size_t)nz * CW;
     const BandCarry<CW, R> C0(RB + (size_t)nz * CW, G), C1(RB + (size_t)nz * CW + ncar, G);
-    // depth profiles: stretch, rhoinv, rho0, gradp0_z, gradrho0_z, g, c2rho0 (1-D case)
-    float *KP = RB + (size_t)nz * CW + 2 * ncar;
-    float *Kst = KP, *Kri = KP + nz, *Kr0 = KP + 2 * nz, *Kgp = KP + 3 * nz, *Kgr = KP + 4 * nz, *Kg = KP + 5 * nz,
-          *Kc2 = KP + 6 * nz;
-    for (int k = threadIdx.x; k < nz; k += blockDim.x) {
-        Kst[k] = Kst[k];
-        Kri[k] = Kri[k];
-        Kr0[k] = Kr0[k];
-        Kgp[k] = Kgp[k];
-        Kgr[k] = Kgr[k];
-        Kg[k] = Kg[k];
-        Kc2[k] = a.c2d ? 0.f : Kc2[k];
+    float *KPB = RB + (size_t)nz * CW + 2 * ncar;
+    float *Kst = KPB, *Kri = KPB + nz, *Kr0 = KPB + 2 * nz, *Kgp = KPB + 3 * nz, *Kgr = KPB + 4 * nz, *Kg = KPB + 5 * nz,
+          *Kc2 = KPB + 6 * nz;
+    for (int k = threadIdx.x; k < nz; k += blockDim.x) {  // depth profiles
+        Kst[k] = __ldg(a.stretch + k);
+        Kri[k] = __ldg(a.rhoinv + k);
+        Kr0[k] = __ldg(a.rho0 + k);
+        Kgp[k] = __ldg(a.gp0 + k);
+        Kgr[k] = __ldg(a.gr0 + k);
+        Kg[k] = __ldg(a.g + k);
+        Kc2[k] = a.c2d ? 0.f : __ldg(a.c2rho0 + k);
     }
     const int c = threadIdx.x % CW, g = threadIdx.x / CW;
     const int x = blockIdx.x * CW + c;
@@ -399,8 +223,7 @@ template <int CW, int R>
 static size_t band_smem(int nz)
 {
     const int G = (nz + R - 1) / R;
-    return ((size_t)4 * nz * CW + 2 * ((size_t)2 * G * CW + BandCarry<CW, R>::floats_fixed()) + (size_t)7 * nz) *
-           sizeof(float);
+    return ((size_t)4 * nz * CW + 2 * ((size_t)2 * G * CW + BandCarry<CW, R>::floats_fixed()) + (size_t)7 * nz) * sizeof(float);
 }
 
 size_t col_band_smem_bytes(int nz, int R, int cw)

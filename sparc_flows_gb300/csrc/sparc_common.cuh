@@ -101,6 +101,7 @@ struct BandDev {
     const float *uv[3];
 };
 
+
 // ------------------------------------------------------------------------------------------
 // FFT
 // ------------------------------------------------------------------------------------------
@@ -410,6 +411,10 @@ size_t col_band_smem_bytes(int nz, int R, int cw);
 int col_band_rows(int nz, int cw);  // rows per thread group (0: no banded pass for this depth / width)
 
 struct ColMaps;
+template <int R>
+cudaError_t launch_col_stage_band_tma(const ColMaps &maps, const StepArgs<float> &a, const BandDev &bd, cudaStream_t st);
+size_t col_band_tma_smem_bytes(int nz, int R, int boxr);
+int col_band_tma_rows(int nz);  // rows per thread group of the TMA-staged banded pass (0: unavailable)
 template <typename T>
 cudaError_t launch_col_stage_tma(const ColMaps &maps, const StepArgs<T> &a, cudaStream_t st);
 template <typename T>

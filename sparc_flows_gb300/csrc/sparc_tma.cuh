@@ -66,6 +66,13 @@ __device__ __forceinline__ void tma_load_2d(void *smem_dst, const CUtensorMap *m
         : "memory");
 }
 
+// Make this thread's generic-proxy shared-memory accesses visible to / ordered before later
+// async-proxy (TMA) operations on the same shared memory.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // The tensor maps one column pass reads (2-D views [rows][nx] of x-fastest fields).
 struct ColMaps {
     CUtensorMap A;    // rows (b*4 + f)*nz + k
@@ -73,6 +80,8 @@ struct ColMaps {
     CUtensorMap DX;   // rows b*nz + k
     CUtensorMap FXX;
     CUtensorMap FXZ;
+    CUtensorMap C2R;  // rows b*nz + k (per-solve background) or k (shared)
+    CUtensorMap V0Z;  // as C2R
 };
 
 }  // namespace sparc

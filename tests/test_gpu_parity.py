@@ -154,18 +154,34 @@ def test_graph_replay_equals_stream_launches():
     assert np.array_equal(a, b)
 
 
-def test_fp32_tracks_fp64():
+@pytest.fixture(scope="module")
+def fp64_300():
     run, model, psi, cmul = make_case(nx=256, nsteps=300, length=400e8)
     spec = M.SourceSpec(0.0)
     w64 = gpu_solver(run, model, psi, cmul, precision=64)
     w64.set_forward_sources([spec])
     s64 = w64.forward().cpu().numpy()
+    st64 = w64.state().cpu().numpy()
     w64.close()
+    return (run, model, psi, cmul, spec), s64, st64
+
+
+# column pass variants of FP32 plans: 0 partitioned solve, 1 partitioned solve with TMA tiles,
+# 2 geometric band, 3 geometric band with TMA tiles; every block width of the banded pass
+@pytest.mark.parametrize("impl,cw", [(0, 32), (1, 32), (2, 32), (2, 16), (2, 8), (3, 32)])
+def test_fp32_tracks_fp64(fp64_300, monkeypatch, impl, cw):
+    (run, model, psi, cmul, spec), s64, st64 = fp64_300
+    monkeypatch.setenv("SPARC_COLUMN_IMPL", str(impl))
+    monkeypatch.setenv("SPARC_COLUMN_BLOCK", str(cw))
     w32 = gpu_solver(run, model, psi, cmul, precision=32)
     w32.set_forward_sources([spec])
     s32 = w32.forward().cpu().numpy()
+    st32 = w32.state().cpu().numpy()
+    w32.check()  # raises on a TMA time-out flag or a non-finite state
     w32.close()
     assert rel_l2(s32, s64) < FP32_TOL
+    for f in range(4):
+        assert rel_l2(st32[0, f], st64[0, f]) < 10 * FP32_TOL, f
 
 
 def test_state_check_detects_divergence():
