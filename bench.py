@@ -38,6 +38,29 @@ def words_per_point_step(nx, nz, npmlbot=20, npmltop=10, npmlhor=9, V=4, B=3):
     return 15 * V + 10 + 5 * B + 15 * naux / (nx * nz)
 
 
+def column_words_per_point(nz, c2d=True, flows=True, npmlbot=20, npmltop=10, bg_shared_by=1):
+    """Algorithmic words per grid point of one column-pass launch (one RK stage), averaged over
+    the five stages: reads xi_z, v_z, v_x, dxi_x/dx, and with flows FXX, FXZ; the 2-D background
+    c2rho0 and v0z (once per launch when the bg_shared_by solves of the batch share it); the RHS
+    ring tiles (rhs v_z of stage s-2 in stages 3-5, rhs v_x and v_z of stage s-1 in stages 2-5);
+    writes p, the partial RHS of v_x and rhs v_z; PML rows add psi_vz and psi_p (state read,
+    ring read in stages 2-5, ring write) and az, bz, fdz."""
+    bg = ((1 if c2d else 0) + (1 if flows else 0)) / bg_shared_by
+    reads = 4 + (2 if flows else 0) + bg + 3 / 5 + 2 * 4 / 5
+    writes = 3
+    pml = (npmlbot + npmltop) / nz * (2 * (1 + 4 / 5 + 1) + 3)
+    return reads + writes + pml
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (None if absent)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f)[kernel]["dram_bytes_per_launch"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
 
@@ -258,11 +281,22 @@ def run_gpu(args):
     e2e_ms = float(te.item())
     e2e_value = pipe.point_steps() * e2e_steps * world / (e2e_ms * 1e-3)
 
+    # ---- accuracy of the FP32 batched path against FP64 on one source of the same workload
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        from sparc_flows_gb300.accuracy import fp32_vs_fp64
+        accuracy = fp32_vs_fp64("batch32", source=15, nsteps=run.nsteps, device=dev)
+
     if rank == 0:
         words = words_per_point_step(run.nx, run.nz)
         peak, peak_kind = measured_peak_hbm()
-        achieved = words * 4 * value / world / 1e9  # GB/s on one GPU
+        achieved = words * 4 * value / world / 1e9  # GB/s on one GPU, whole step
         dom = max(passes["per_class_ms"], key=passes["per_class_ms"].get)
+        # dominant kernel: the column pass, five launches per step, timed with CUDA events
+        col_launch_ms = passes["per_class_ms"]["column"] / 5
+        col_bytes = column_words_per_point(run.nz, bg_shared_by=len(specs)) * 4 * len(specs) * run.nx * run.nz
+        col_achieved = col_bytes / (col_launch_ms * 1e-3) / 1e9
+        col_kernel = pipe.fwd.column_kernel_name()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -271,12 +305,14 @@ def run_gpu(args):
                        "nsteps": run.nsteps, "step": "forward + adjoint + kernel integral of all sources",
                        "l2": "inputs larger than L2 (working set ~0.4 GB state + 28 GB partial states per GPU)",
                        "parallelism": f"replicas x{world} (sources sharded, no collective)"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": "one RK time step (12 launches, CUDA graph)",
-                         "algorithmic_bytes_per_point_step": words * 4, "peak_kind": peak_kind,
-                         "dominant_kernel": dom, "pass_ms_per_step": passes["per_class_ms"],
-                         "pass_share": passes["share"]},
+            "roofline": {"bound": "hbm", "achieved": col_achieved, "peak": peak, "unit": "GB/s",
+                         "frac": col_achieved / peak, "traffic": ncu_traffic(col_kernel),
+                         "kernel": col_kernel, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": col_bytes, "launch_ms": col_launch_ms,
+                         "step": {"achieved": achieved, "frac": achieved / peak,
+                                  "algorithmic_bytes_per_point_step": words * 4,
+                                  "dominant_pass": dom, "pass_ms_per_step": passes["per_class_ms"],
+                                  "pass_share": passes["share"]}},
             "clocks": clk.summary(),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps},
@@ -285,6 +321,8 @@ def run_gpu(args):
         if plain is not None:
             plain["fp32_batched_over_fp64_plain"] = (value / world) / plain["value"]
             line["fp64_plain"] = plain
+        if accuracy is not None:
+            line["accuracy"] = accuracy
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_quick()
         print(json.dumps(line), flush=True)
@@ -302,6 +340,7 @@ def main():
     ap.add_argument("--nsteps", type=int, default=0, help="override the 3600 time steps (testing only)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain reference path")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy report")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

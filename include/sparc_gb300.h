@@ -146,6 +146,10 @@ int sparc_check_state(sparc_plan_t *plan, double *norms, void *stream);
 /* Current step counter (synchronises the stream). */
 int sparc_get_time(sparc_plan_t *plan, int *time, void *stream);
 
+/* Diagnostics (no counterpart in the reference): the kernels this plan launches for its column
+ * and end-of-step passes, as "column=<kernel> end=<kernel>" (NUL-terminated, at most len bytes). */
+int sparc_plan_describe(const sparc_plan_t *plan, char *buf, int len);
+
 /* Kernel construction from paired snapshots (kernels.f90:209-358): for record pair
  * (j, jadj = nadj-1-j), j = 0..npair-1, accumulate in FP64
  *   kc  += div(f_xi) * div(a_v),  kvx += d_x(f_v) . a_v,  kvz += d_z(f_v) . a_v,

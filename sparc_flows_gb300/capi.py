@@ -36,6 +36,7 @@ SIGNATURES = {
     "sparc_profile_passes": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _vp]),
     "sparc_check_state": (ctypes.c_int, [_vp, _dp, _vp]),
     "sparc_get_time": (ctypes.c_int, [_vp, _ip, _vp]),
+    "sparc_plan_describe": (ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int]),
     "sparc_kernels": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_kernels_accumulate": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_kernels_accumulate_static": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),

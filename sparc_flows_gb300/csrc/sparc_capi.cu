@@ -1088,6 +1088,28 @@ int sparc_check_state(sparc_plan_t *p, double *norms, void *stream)
     return SPARC_OK;
 }
 
+int sparc_plan_describe(const sparc_plan_t *p, char *buf, int len)
+{
+    if (!p || !buf || len < 1) return fail(SPARC_ERR_ARG, "sparc_plan_describe: bad argument");
+    std::string col, end;
+    if (p->cfg.precision == 32) {
+        const Solver<float> &S = p->s32;
+        if (S.band_tma_R) col = "col_band_tma_kernel<" + std::to_string(S.band_tma_R) + ">";
+        else if (S.band_R) col = "col_band_kernel<" + std::to_string(S.band_cw) + "," + std::to_string(S.band_R) + ">";
+        else if (S.have_maps && p->cfg.column_impl == 1) col = "col_stage_tma_kernel<float>";
+        else col = "col_stage_kernel<float," + std::to_string(S.a.colw) + ">";
+        end = (S.have_maps && !S.a.ALO) ? "end_step_tma_kernel<float>" : "end_step_kernel<float>";
+    } else {
+        const Solver<double> &S = p->s64;
+        col = (S.have_maps && p->cfg.column_impl == 1) ? "col_stage_tma_kernel<double>"
+                                                        : "col_stage_kernel<double," + std::to_string(S.a.colw) + ">";
+        end = S.have_maps ? "end_step_tma_kernel<double>" : "end_step_kernel<double>";
+    }
+    const std::string d = "column=" + col + " end=" + end;
+    std::snprintf(buf, (size_t)len, "%s", d.c_str());
+    return SPARC_OK;
+}
+
 int sparc_get_time(sparc_plan_t *p, int *time, void *stream)
 {
     if (!p || !time) return fail(SPARC_ERR_ARG, "sparc_get_time: bad argument");
