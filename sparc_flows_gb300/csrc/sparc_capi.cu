@@ -1095,7 +1095,12 @@ int sparc_plan_describe(const sparc_plan_t *p, char *buf, int len)
     if (p->cfg.precision == 32) {
         const Solver<float> &S = p->s32;
         if (S.band_tma_R) col = "col_band_tma_kernel<" + std::to_string(S.band_tma_R) + ">";
-        else if (S.band_R) col = "col_band_kernel<" + std::to_string(S.band_cw) + "," + std::to_string(S.band_R) + ">";
+        else if (S.band_R)
+            col = "col_band_kernel<" + std::to_string(S.band_cw) + "," + std::to_string(S.band_R) + "," +
+                  (col_band_specialised(p->cfg.nx, p->cfg.nz, S.band_cw, S.band_R)
+                       ? std::to_string(p->cfg.nx) + "," + std::to_string(p->cfg.nz)
+                       : std::string("0,0")) +
+                  ">";
         else if (S.have_maps && p->cfg.column_impl == 1) col = "col_stage_tma_kernel<float>";
         else col = "col_stage_kernel<float," + std::to_string(S.a.colw) + ">";
         end = (S.have_maps && !S.a.ALO) ? "end_step_tma_kernel<float>" : "end_step_kernel<float>";

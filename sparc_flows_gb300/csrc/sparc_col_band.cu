@@ -11,11 +11,14 @@
 
 namespace sparc {
 
-template <int CW, int R>
+// NX, NZ: the grid as compile-time constants (0: taken from the arguments).  With them every
+// global and shared-memory offset of the unrolled row loops is an immediate, and with NZ a
+// multiple of R every thread group is full; the generic instantiation serves other grids.
+template <int CW, int R, int NX, int NZ>
 __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band_kernel(StepArgs<float> a, BandDev bd)
 {
     extern __shared__ __align__(16) float smb[];
-    const int nz = a.nz, nx = a.nx;
+    const int nz = NZ ? NZ : a.nz, nx = NX ? NX : a.nx;
     const int G = blockDim.x / CW;
     const int ncar = 2 * G * CW + BandCarry<CW, R>::floats_fixed();
     float *FA = smb;
@@ -39,7 +42,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     const int x = blockIdx.x * CW + c;
     const int b = blockIdx.y;
     const int k0 = g * R;
-    const int n = min(R, nz - k0);
+    const int n = (NZ && NZ % R == 0) ? R : min(R, nz - k0);
     const size_t F = (size_t)nz * nx;
     const float *Ab = a.A + (size_t)b * 4 * F;
     const int s = a.stage;
@@ -242,18 +245,43 @@ size_t col_band_smem_bytes(int nz, int R, int cw)
     }
 }
 
-template <int CW, int R>
-cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st)
+template <int CW, int R, int NX, int NZ>
+static cudaError_t launch_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st)
 {
     const int G = (a.nz + R - 1) / R;
     if (G > band_maxg<CW>() || a.nx % CW != 0 || R * G - a.nz >= R) return cudaErrorInvalidValue;
+    if ((NX && a.nx != NX) || (NZ && a.nz != NZ)) return cudaErrorInvalidValue;
     const size_t smem = band_smem<CW, R>(a.nz);
-    cudaError_t e =
-        cudaFuncSetAttribute(col_band_kernel<CW, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(col_band_kernel<CW, R, NX, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid(a.nx / CW, a.nb);
-    col_band_kernel<CW, R><<<grid, G * CW, smem, st>>>(a, bd);
+    col_band_kernel<CW, R, NX, NZ><<<grid, G * CW, smem, st>>>(a, bd);
     return cudaGetLastError();
+}
+
+// Grids with a compiled specialisation: nz = 300 (the reference's params.i depth) with the
+// 32-column, 10-row geometry and nx = 128 .. 1024.
+bool col_band_specialised(int nx, int nz, int cw, int R)
+{
+    return cw == 32 && R == 10 && nz == 300 && (nx == 128 || nx == 256 || nx == 512 || nx == 1024);
+}
+
+template <int CW, int R>
+cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st)
+{
+    if constexpr (CW == 32 && R == 10) {
+        if (a.nz == 300) {
+            switch (a.nx) {
+                case 128: return launch_band<32, 10, 128, 300>(a, bd, st);
+                case 256: return launch_band<32, 10, 256, 300>(a, bd, st);
+                case 512: return launch_band<32, 10, 512, 300>(a, bd, st);
+                case 1024: return launch_band<32, 10, 1024, 300>(a, bd, st);
+                default: break;
+            }
+        }
+    }
+    return launch_band<CW, R, 0, 0>(a, bd, st);
 }
 
 #define SPARC_BAND_INST(cw, r) \

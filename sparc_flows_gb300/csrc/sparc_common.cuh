@@ -408,6 +408,7 @@ bool fft_size_supported(int n);
 template <int CW, int R>
 cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st);
 size_t col_band_smem_bytes(int nz, int R, int cw);
+bool col_band_specialised(int nx, int nz, int cw, int R);  // compiled for this grid
 int col_band_rows(int nz, int cw);  // rows per thread group (0: no banded pass for this depth / width)
 
 struct ColMaps;
