@@ -472,6 +472,7 @@ struct Solver {
     int band_R = 0;    // rows per thread group of the banded column pass (0: not used)
     int band_cw = 0;   // its block width (columns)
     int band_tma_R = 0;  // rows per thread group of the TMA-staged banded pass (0: not used)
+    bool end_stream = false;  // streamed end-of-step kernel (32-column tiles) fits this grid
     std::vector<void *> allocs;
     size_t F = 0;
     T *work = nullptr;  // kernel-accumulation scratch [nb][8][nz][nx]
@@ -582,6 +583,12 @@ int alloc_solver(sparc_plan *p)
     a.colw = (c.column_block != 8 && nx % 32 == 0) ? 32 : 8;
     a.inj_scale = inj; a.src_rows = rows; a.nrows = 1;
     a.d_err = p->d_err;
+    {  // streamed end-of-step kernel: two [nz][32] fields in shared memory
+        int maxsm = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        S.end_stream = nx % 32 == 0 && end_stream_smem_bytes<T>(nz) <= (size_t)maxsm;
+    }
     // banded column pass (FP32 only: its truncation at 5e-10 is below FP32 rounding, not FP64's)
     S.band_R = 0;
     const int bcw = (c.column_block == 8 || c.column_block == 16 || c.column_block == 32) ? c.column_block : 16;
@@ -683,7 +690,9 @@ template <typename T>
 cudaError_t end_step(sparc_plan *p, const StepArgs<T> &a, cudaStream_t st)
 {
     Solver<T> &S = solver<T>(p);
-    return (S.have_maps && !a.ALO) ? launch_end_step_tma<T>(S.maps, a, st) : launch_end_step<T>(a, st);
+    if (a.ALO) return launch_end_step<T>(a, st);  // compensated (double-float) update
+    if (S.have_maps && p->cfg.column_impl == 1) return launch_end_step_tma<T>(S.maps, a, st);
+    return S.end_stream ? launch_end_step_stream<T>(a, st) : launch_end_step<T>(a, st);
 }
 
 template <typename T>
@@ -1103,12 +1112,15 @@ int sparc_plan_describe(const sparc_plan_t *p, char *buf, int len)
                   ">";
         else if (S.have_maps && p->cfg.column_impl == 1) col = "col_stage_tma_kernel<float>";
         else col = "col_stage_kernel<float," + std::to_string(S.a.colw) + ">";
-        end = (S.have_maps && !S.a.ALO) ? "end_step_tma_kernel<float>" : "end_step_kernel<float>";
+        end = S.a.ALO ? "end_step_kernel<float>"
+                      : (S.have_maps && p->cfg.column_impl == 1) ? "end_step_tma_kernel<float>"
+                      : S.end_stream ? "end_step_stream_kernel<float>" : "end_step_kernel<float>";
     } else {
         const Solver<double> &S = p->s64;
         col = (S.have_maps && p->cfg.column_impl == 1) ? "col_stage_tma_kernel<double>"
                                                         : "col_stage_kernel<double," + std::to_string(S.a.colw) + ">";
-        end = S.have_maps ? "end_step_tma_kernel<double>" : "end_step_kernel<double>";
+        end = (S.have_maps && p->cfg.column_impl == 1) ? "end_step_tma_kernel<double>"
+              : S.end_stream ? "end_step_stream_kernel<double>" : "end_step_kernel<double>";
     }
     const std::string d = "column=" + col + " end=" + end;
     std::snprintf(buf, (size_t)len, "%s", d.c_str());

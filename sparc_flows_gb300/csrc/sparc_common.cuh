@@ -411,6 +411,11 @@ size_t col_band_smem_bytes(int nz, int R, int cw);
 bool col_band_specialised(int nx, int nz, int cw, int R);  // compiled for this grid
 int col_band_rows(int nz, int cw);  // rows per thread group (0: no banded pass for this depth / width)
 
+template <typename T>
+cudaError_t launch_end_step_stream(const StepArgs<T> &a, cudaStream_t st);
+template <typename T>
+size_t end_stream_smem_bytes(int nz);
+
 struct ColMaps;
 template <int R>
 cudaError_t launch_col_stage_band_tma(const ColMaps &maps, const StepArgs<float> &a, const BandDev &bd, cudaStream_t st);
