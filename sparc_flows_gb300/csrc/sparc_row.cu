@@ -8,13 +8,122 @@
 //   d/dx of xi_x at stage s    -> divergence input of stage s (plus the top-row value that
 //                                 the column pass needs for its ibc=3 boundary);
 //   d/dx of v_x, v_z at stage s -> advection terms -2 v0x d/dx (physics2d.f90:1065-1079).
-#include "sparc_common.cuh"
+#include "sparc_fft512.cuh"
 
 namespace sparc {
 
 constexpr int ROW_WPB = 4;  // rows (warps) per block
 
-// MODE 0: stage 1 (no pressure yet), MODE 1: stages 2..5, MODE 2: closing pass after stage 5.
+// Per-row state of a row pass and its three per-column steps, shared by the Stockham kernel and
+// the register-FFT kernel.  MODE 0: stage 1 (no pressure yet), MODE 1: stages 2..5, MODE 2:
+// closing pass after stage 5.
+template <typename T>
+struct RowCtx {
+    int b, k, nx, nh, nhx;
+    size_t F, ro;
+    const T *Ab;
+    T bs, bsm1, rhoinv_k;
+    T *PXb;
+    const T *axk, *bxk;
+    __device__ RowCtx(const StepArgs<T> &a, int row, int N)
+    {
+        b = row / a.nz;
+        k = row - b * a.nz;
+        nx = N;
+        nh = a.nh;
+        nhx = a.nhx;
+        F = (size_t)a.nz * nx;
+        ro = (size_t)k * nx;
+        Ab = a.A + (size_t)b * 4 * F;
+        bs = a.bs;
+        bsm1 = a.bsm1;
+        rhoinv_k = __ldg(a.rhoinv + k);
+        PXb = a.PX + (size_t)b * 2 * a.nz * nhx;
+        axk = a.ax + (size_t)b * a.bgx + (size_t)k * nhx;
+        bxk = a.bx + (size_t)b * a.bgx + (size_t)k * nhx;
+    }
+};
+
+// Inputs of the first FFT at column x: (p_{s-1}, xi_x at stage s) or (p_5, 0).
+template <typename T, int MODE>
+__device__ __forceinline__ void row_load(const StepArgs<T> &a, const RowCtx<T> &r, int x, T &p, T &xis)
+{
+    const int b = r.b, k = r.k;
+    const size_t F = r.F, ro = r.ro;
+    p = T(0);
+    xis = T(0);
+    if (MODE != 0) p = __ldg(a.P + (size_t)b * F + ro + x);
+    if (MODE == 0) {
+        xis = __ldg(r.Ab + F_XIX * F + ro + x);
+    } else if (MODE == 1) {
+        T avx = __ldg(r.Ab + F_VX * F + ro + x);
+        T s = (a.stage == 2) ? avx : avx + r.bsm1 * __ldg(svp(a, a.slot_sm2, b, 0) + ro + x);
+        if (k == 0 || x == 0 || x == r.nx - 1) s = T(0);  // RHS boundary zeros (physics2d.f90:1083-1093)
+        xis = __ldg(r.Ab + F_XIX * F + ro + x) + r.bs * s;
+    }
+}
+
+// From gpx = dp/dx and dxx = dxi_x/dx at column x: x-PML, RHS v_x of stage s-1, dxi_x/dx for the
+// column pass; the inputs (v_x, v_z at stage s) of the second FFT (MODE != 2).
+template <typename T, int MODE>
+__device__ __forceinline__ void row_mid(const StepArgs<T> &a, const RowCtx<T> &r, int x, T gpx, T dxx, T &vxs, T &vzs)
+{
+    const int b = r.b, k = r.k, nx = r.nx, nh = r.nh, nhx = r.nhx;
+    const size_t F = r.F, ro = r.ro;
+    const bool pml = (x < nh) || (x >= nx - nh);
+    const int ai = (x < nh) ? x : x - (nx - nh) + nh;
+    if (MODE != 2 && k == a.nz - 1) a.TOPDX[(size_t)b * nx + x] = dxx;
+    if (pml) {
+        const T axv = __ldg(r.axk + ai), bxv = __ldg(r.bxk + ai);
+        if (MODE != 0) {  // psi_gradp_x of stage s-1
+            const size_t q = ((size_t)1 * a.nz + k) * nhx + ai;
+            T ps = r.PXb[q];
+            if (a.stage >= 3) ps += r.bsm1 * a.SPX[((size_t)a.slot_sm2 * a.nb + b) * 2 * a.nz * nhx + q];
+            gpx += ps;
+            a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q] = axv * gpx + bxv * ps;
+        }
+        if (MODE != 2) {  // psi_vx of stage s
+            const size_t q = ((size_t)0 * a.nz + k) * nhx + ai;
+            T ps = r.PXb[q];
+            if (MODE == 1) ps += r.bs * a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q];
+            dxx += ps;
+            a.SPX[((size_t)a.slot_s * a.nb + b) * 2 * a.nz * nhx + q] = axv * dxx + bxv * ps;
+        }
+    }
+    T svx = T(0);
+    if (MODE != 0) {
+        svx = __ldg(a.RVXP + (size_t)b * F + ro + x) - r.rhoinv_k * gpx;
+        if (k == 0 || x == 0 || x == nx - 1) svx = T(0);
+        svp(a, a.slot_sm1, b, 0)[ro + x] = svx;
+    }
+    vxs = T(0);
+    vzs = T(0);
+    if (MODE != 2) {
+        a.DX[(size_t)b * F + ro + x] = dxx;
+        vxs = __ldg(r.Ab + F_VX * F + ro + x);
+        vzs = __ldg(r.Ab + F_VZ * F + ro + x);
+        if (MODE == 1) {
+            vxs += r.bs * svx;
+            vzs += r.bs * __ldg(svp(a, a.slot_sm1, b, 1) + ro + x);
+        }
+    } else if (pml) {
+        // closing pass: pmlvarsx += deltat * scrpmlx (step.f90:112-115)
+        for (int c = 0; c < 2; c++) {
+            const size_t q = ((size_t)c * a.nz + k) * nhx + ai;
+            r.PXb[q] += a.dt * a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q];
+        }
+    }
+}
+
+// x-advection terms -2 v0x d/dx of v_x, v_z at column x.
+template <typename T>
+__device__ __forceinline__ void row_out(const StepArgs<T> &a, const RowCtx<T> &r, int x, T dvx, T dvz)
+{
+    const T w = T(-2) * a.fsign * __ldg(a.v0x + (size_t)r.b * a.bg2 + r.ro + x);
+    a.FXX[(size_t)r.b * r.F + r.ro + x] = w * dvx;
+    a.FXZ[(size_t)r.b * r.F + r.ro + x] = w * dvz;
+}
+
 template <typename T, int N, int MODE>
 __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
 {
@@ -25,30 +134,12 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
     const int row = blockIdx.x * ROW_WPB + warp;
     if (row >= a.nb * a.nz) return;
     T *xr = sm + warp * 4 * N, *xi = xr + N, *yr = xi + N, *yi = yr + N;
-    const int b = row / a.nz, k = row - b * a.nz;
-    const int nx = N, nh = a.nh, nhx = a.nhx;
-    const size_t F = (size_t)a.nz * nx;
-    const size_t ro = (size_t)k * nx;
-    const T *Ab = a.A + (size_t)b * 4 * F;
-    const T bs = a.bs, bsm1 = a.bsm1;
-    const T rhoinv_k = __ldg(a.rhoinv + k);
-    T *PXb = a.PX + (size_t)b * 2 * a.nz * nhx;
-    const T *axk = a.ax + (size_t)b * a.bgx + (size_t)k * nhx;
-    const T *bxk = a.bx + (size_t)b * a.bgx + (size_t)k * nhx;
+    const RowCtx<T> r(a, row, N);
 
-    // ---- load: (p_{s-1}, xi_x at stage s) or (p_5, 0)
     T mr = T(0), mi = T(0);
-    for (int x = lane; x < nx; x += WARP) {
-        T p = T(0), xis = T(0);
-        if (MODE != 0) p = __ldg(a.P + (size_t)b * F + ro + x);
-        if (MODE == 0) {
-            xis = __ldg(Ab + F_XIX * F + ro + x);
-        } else if (MODE == 1) {
-            T avx = __ldg(Ab + F_VX * F + ro + x);
-            T s = (a.stage == 2) ? avx : avx + bsm1 * __ldg(svp(a, a.slot_sm2, b, 0) + ro + x);
-            if (k == 0 || x == 0 || x == nx - 1) s = T(0);  // RHS boundary zeros (physics2d.f90:1083-1093)
-            xis = __ldg(Ab + F_XIX * F + ro + x) + bs * s;
-        }
+    for (int x = lane; x < N; x += WARP) {
+        T p, xis;
+        row_load<T, MODE>(a, r, x, p, xis);
         xr[x] = p;
         xi[x] = xis;
         mr = fmax(mr, fabs(p));
@@ -63,51 +154,14 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
     __syncwarp();
 
     T mr2 = T(0), mi2 = T(0);
-    for (int x = lane; x < nx; x += WARP) {
-        T gpx = o1r[x] * isr, dxx = o1i[x] * isi;
-        const bool pml = (x < nh) || (x >= nx - nh);
-        const int ai = (x < nh) ? x : x - (nx - nh) + nh;
-        if (MODE != 2 && k == a.nz - 1) a.TOPDX[(size_t)b * nx + x] = dxx;
-        if (pml) {
-            const T axv = __ldg(axk + ai), bxv = __ldg(bxk + ai);
-            if (MODE != 0) {  // psi_gradp_x of stage s-1
-                const size_t q = ((size_t)1 * a.nz + k) * nhx + ai;
-                T ps = PXb[q];
-                if (a.stage >= 3) ps += bsm1 * a.SPX[((size_t)a.slot_sm2 * a.nb + b) * 2 * a.nz * nhx + q];
-                gpx += ps;
-                a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q] = axv * gpx + bxv * ps;
-            }
-            if (MODE != 2) {  // psi_vx of stage s
-                const size_t q = ((size_t)0 * a.nz + k) * nhx + ai;
-                T ps = PXb[q];
-                if (MODE == 1) ps += bs * a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q];
-                dxx += ps;
-                a.SPX[((size_t)a.slot_s * a.nb + b) * 2 * a.nz * nhx + q] = axv * dxx + bxv * ps;
-            }
-        }
-        T svx = T(0);
-        if (MODE != 0) {
-            svx = __ldg(a.RVXP + (size_t)b * F + ro + x) - rhoinv_k * gpx;
-            if (k == 0 || x == 0 || x == nx - 1) svx = T(0);
-            svp(a, a.slot_sm1, b, 0)[ro + x] = svx;
-        }
+    for (int x = lane; x < N; x += WARP) {
+        T vxs, vzs;
+        row_mid<T, MODE>(a, r, x, o1r[x] * isr, o1i[x] * isi, vxs, vzs);
         if (MODE != 2) {
-            a.DX[(size_t)b * F + ro + x] = dxx;
-            T vxs = __ldg(Ab + F_VX * F + ro + x), vzs = __ldg(Ab + F_VZ * F + ro + x);
-            if (MODE == 1) {
-                vxs += bs * svx;
-                vzs += bs * __ldg(svp(a, a.slot_sm1, b, 1) + ro + x);
-            }
             o1r[x] = vxs;
             o1i[x] = vzs;
             mr2 = fmax(mr2, fabs(vxs));
             mi2 = fmax(mi2, fabs(vzs));
-        } else if (pml) {
-            // closing pass: pmlvarsx += deltat * scrpmlx (step.f90:112-115)
-            for (int c = 0; c < 2; c++) {
-                const size_t q = ((size_t)c * a.nz + k) * nhx + ai;
-                PXb[q] += a.dt * a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q];
-            }
         }
     }
     if (MODE == 2 || !a.flows) return;
@@ -119,12 +173,52 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
     T *o2r, *o2i;
     fft_deriv<T, N>(o1r, o1i, gr, gi, a.twr, a.twi, a.kap, a.stretchx, lane, o2r, o2i, sr2, si2);
     __syncwarp();
-    const T *v0xk = a.v0x + (size_t)b * a.bg2 + ro;
-    for (int x = lane; x < nx; x += WARP) {
-        const T w = T(-2) * a.fsign * __ldg(v0xk + x);
-        a.FXX[(size_t)b * F + ro + x] = w * (o2r[x] * isr2);
-        a.FXZ[(size_t)b * F + ro + x] = w * (o2i[x] * isi2);
+    for (int x = lane; x < N; x += WARP) row_out(a, r, x, o2r[x] * isr2, o2i[x] * isi2);
+}
+
+// FP32 rows of 512 columns: the same row pass with the register-resident FFT (sparc_fft512.cuh);
+// register n2 of a lane holds column lane + 32 n2.
+template <int MODE>
+__global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_reg512_kernel(StepArgs<float> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (MODE == 0 && blockIdx.x == 0 && threadIdx.x == 0) *a.d_time += 1;  // new step begins
+    const int row = blockIdx.x * ROW_WPB + warp;
+    if (row >= a.nb * a.nz) return;
+    float *S = reinterpret_cast<float *>(smem_raw) + warp * FFT512_SCRATCH;
+    const RowCtx<float> r(a, row, 512);
+
+    float re[16], im[16];
+    float mr = 0.f, mi = 0.f;
+#pragma unroll
+    for (int n2 = 0; n2 < 16; n2++) {
+        row_load<float, MODE>(a, r, lane + 32 * n2, re[n2], im[n2]);
+        mr = fmaxf(mr, fabsf(re[n2]));
+        mi = fmaxf(mi, fabsf(im[n2]));
     }
+    float sr, si, isr, isi;
+    warp_row_scale(mr, sr, isr);
+    warp_row_scale(mi, si, isi);
+    fft512_deriv(re, im, S, a.twr, a.twi, a.kap, a.stretchx, lane, sr, si);
+
+    float mr2 = 0.f, mi2 = 0.f;
+#pragma unroll
+    for (int n2 = 0; n2 < 16; n2++) {
+        float vxs, vzs;
+        row_mid<float, MODE>(a, r, lane + 32 * n2, re[n2] * isr, im[n2] * isi, vxs, vzs);
+        re[n2] = vxs;
+        im[n2] = vzs;
+        mr2 = fmaxf(mr2, fabsf(vxs));
+        mi2 = fmaxf(mi2, fabsf(vzs));
+    }
+    if (MODE == 2 || !a.flows) return;
+    float sr2, si2, isr2, isi2;
+    warp_row_scale(mr2, sr2, isr2);
+    warp_row_scale(mi2, si2, isi2);
+    fft512_deriv(re, im, S, a.twr, a.twi, a.kap, a.stretchx, lane, sr2, si2);
+#pragma unroll
+    for (int n2 = 0; n2 < 16; n2++) row_out(a, r, lane + 32 * n2, re[n2] * isr2, im[n2] * isi2);
 }
 
 // Generic spectral x-derivative of nrows rows (two rows per warp).
@@ -170,9 +264,23 @@ bool fft_size_supported(int n)
     return false;
 }
 
+template <int MODE>
+static void row_reg512_launch(const StepArgs<float> &a, int grid, cudaStream_t st)
+{
+    const size_t smem = (size_t)ROW_WPB * FFT512_SCRATCH * sizeof(float);
+    row_stage_reg512_kernel<MODE><<<grid, ROW_WPB * WARP, smem, st>>>(a);
+}
+
 template <typename T, int N>
 static cudaError_t row_stage_n(const StepArgs<T> &a, cudaStream_t st)
 {
+    if constexpr (sizeof(T) == 4 && N == 512) {
+        const int grid = (a.nb * a.nz + ROW_WPB - 1) / ROW_WPB;
+        if (a.stage == 1) row_reg512_launch<0>(a, grid, st);
+        else if (a.stage <= 5) row_reg512_launch<1>(a, grid, st);
+        else row_reg512_launch<2>(a, grid, st);
+        return cudaGetLastError();
+    }
     const int rows = a.nb * a.nz;
     const int grid = (rows + ROW_WPB - 1) / ROW_WPB;
     const size_t smem = (size_t)ROW_WPB * 4 * N * sizeof(T);

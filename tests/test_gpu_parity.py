@@ -184,6 +184,24 @@ def test_fp32_tracks_fp64(fp64_300, monkeypatch, impl, cw):
         assert rel_l2(st32[0, f], st64[0, f]) < 10 * FP32_TOL, f
 
 
+def test_fp32_512_columns_track_fp64():
+    """On 512-column grids FP32 row passes use the register-resident FFT (FP64 keeps the
+    Stockham FFT): seismograms and state of 200 steps against FP64."""
+    run, model, psi, cmul = make_case(nx=512, nsteps=200, length=400e8)
+    spec = M.SourceSpec(20.0)
+    out = {}
+    for prec in (64, 32):
+        w = gpu_solver(run, model, psi, cmul, precision=prec)
+        w.set_forward_sources([spec])
+        seis = w.forward().cpu().numpy()
+        out[prec] = (seis, w.state().cpu().numpy())
+        w.check()
+        w.close()
+    assert rel_l2(out[32][0], out[64][0]) < FP32_TOL
+    for f in range(4):
+        assert rel_l2(out[32][1][0, f], out[64][1][0, f]) < 10 * FP32_TOL, f
+
+
 def test_state_check_detects_divergence():
     """Failure detection on the host side of the ABI: a non-finite state (planted through
     sparc_set_state, no device fault) is reported as SPARC_ERR_NONFINITE; a healthy state's norm
