@@ -214,3 +214,37 @@ def workload(name: str):
         srcs = [SourceSpec(-200.0 + 12.5 * (s + 0.5)) for s in range(32)]
         return run, model, srcs, psi, c_bump(run, model)
     raise KeyError(name)
+
+
+# --------------------------------------------------------------------------------------
+# The uneven batch: solves of different grids, lengths and backgrounds
+# --------------------------------------------------------------------------------------
+@dataclasses.dataclass
+class Solve:
+    """One independent solve of the uneven batch."""
+    nx: int
+    nsteps: int
+    vpeak_ms: float      # flow amplitude (max |v0x| of the supergranule stream function)
+    dcc: float           # sound-speed bump amplitude dc/c
+    xloc: float          # source position, Mm from the box centre
+
+
+def uneven_solves(n: int = 48, seed: int = 0) -> list[Solve]:
+    """n solves, seeded: nx ~ U{256, 384, 512} (0.78125 Mm spacing, so 200 / 300 / 400 Mm boxes),
+    steps ~ U{1800, 2700, 3600}, flow amplitude ~ U(0, 300) m/s, dc/c ~ U(0, 0.05), the flow and
+    bump shapes of the batch32 workload, source positions uniform over the inner 80 % of the box."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        nx = int(rng.choice([256, 384, 512]))
+        steps = int(rng.choice([1800, 2700, 3600]))
+        vpeak = float(rng.uniform(0.0, 300.0))
+        dcc = float(rng.uniform(0.0, 0.05))
+        xloc = float(rng.uniform(-0.4, 0.4)) * nx * 0.78125
+        out.append(Solve(nx, steps, vpeak, dcc, xloc))
+    return out
+
+
+def uneven_run(nx: int, nsteps: int) -> RunConfig:
+    """Run configuration of one group of the uneven batch (batch32 physics, 20-layer bottom PML)."""
+    return RunConfig(nx=nx, nz=300, xlength_cm=nx * 0.78125e8, nsteps=nsteps, flows=True, npmlbot=20)

@@ -287,7 +287,7 @@ class WaveSolver:
                                            w.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                            ix.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(ix), _stream()),
                    "sparc_set_source")
-        torch.cuda.synchronize(self.dev)
+        torch.cuda.current_stream(self.dev).synchronize()  # host tables outlive the copies
 
     def update_flow(self, psi: torch.Tensor):
         """New stream function (nz, nx) in Mm, a device tensor: recompute v0 on the GPU

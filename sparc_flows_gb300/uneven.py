@@ -1,0 +1,81 @@
+"""The uneven batch: independent solves of different grids, lengths and backgrounds.
+
+Solves sharing (nx, steps) form one batched plan (per-solve stream function and sound-speed
+multiplier, a per-solve background in HBM); the groups run concurrently, each from its own host
+thread on its own CUDA stream, so that small groups fill the GPU together.  The reference runs
+every solve as its own single-rank ``sparc`` process (data_forward.sh:28).
+"""
+from __future__ import annotations
+
+import threading
+
+import numpy as np
+import torch
+
+from . import model as M
+from .pipeline import FwdAdjKernels, receiver_columns
+
+
+def group_solves(solves: list) -> dict:
+    """{(nx, nsteps): [indices into solves]}"""
+    groups: dict = {}
+    for i, s in enumerate(solves):
+        groups.setdefault((s.nx, s.nsteps), []).append(i)
+    return groups
+
+
+class UnevenBatch:
+    def __init__(self, solves: list, precision: int = 32, device: str = "cuda:0"):
+        self.solves, self.dev = solves, torch.device(device)
+        model = M.polytrope(300)
+        self.groups = group_solves(solves)
+        self.pipes, self.streams = {}, {}
+        for key, idx in self.groups.items():
+            nx, nsteps = key
+            run = M.uneven_run(nx, nsteps)
+            psis, cmuls, specs = [], [], []
+            for i in idx:
+                s = solves[i]
+                psis.append(M.gaussian_psi(run, model, M.psi_amplitude_for_peak(run, model, 1.0)) * s.vpeak_ms)
+                cmuls.append(M.c_bump(run, model, amp=s.dcc))
+                specs.append(M.SourceSpec(s.xloc))
+            half = 0.45 * nx * 0.78125
+            rcv = receiver_columns(run, n=int(2 * half / 2.0), x0=-half, dx=2.0)
+            self.pipes[key] = FwdAdjKernels(run, model, specs, psi=psis, cmul=cmuls, precision=precision,
+                                            receivers=rcv, device=device)
+            self.streams[key] = torch.cuda.Stream(device=self.dev)
+
+    def point_steps(self) -> int:
+        """Useful grid-point steps of one run (forward and adjoint counted once each)."""
+        return sum(2 * s.nx * 300 * s.nsteps for s in self.solves)
+
+    def run(self):
+        """Forward + adjoint + kernel integral of every solve; groups concurrently."""
+        errors = []
+
+        def work(key):
+            try:
+                with torch.cuda.device(self.dev), torch.cuda.stream(self.streams[key]):
+                    self.pipes[key].run_all()
+                self.streams[key].synchronize()
+            except Exception as e:  # reported after the join
+                errors.append((key, e))
+
+        threads = [threading.Thread(target=work, args=(k,)) for k in self.pipes]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        if errors:
+            raise RuntimeError(f"uneven batch group {errors[0][0]} failed: {errors[0][1]}")
+
+    def seismograms(self, i: int) -> torch.Tensor:
+        """Seismograms (nrec, nx) of solve i from the last run."""
+        for key, idx in self.groups.items():
+            if i in idx:
+                return self.pipes[key].seis[idx.index(i)]
+        raise IndexError(i)
+
+    def close(self):
+        for p in self.pipes.values():
+            p.close()
