@@ -23,18 +23,23 @@ template <int R>
 constexpr int band_gt() { return (BAND_KC + R - 1) / R + 1; }  // ... the top corner
 
 // Shared carries of one derivative: CL, CU [G][CW], corner partial products PB [GB][Q][CW],
-// PT [GT][Q][CW].
+// PT [GT][Q][CW], and the top-block Thomas workspace YT [GT][KC][CW].
 template <int CW, int R>
 struct BandCarry {
     float *CL, *CU, *PB, *PT;
+    float *YT;  // top-block Thomas workspace [GT][KC][CW] (each thread its own column)
     __device__ BandCarry(float *base, int G)
     {
         CL = base;
         CU = CL + G * CW;
         PB = CU + G * CW;
         PT = PB + band_gb<R>() * BAND_Q * CW;
+        YT = PT + band_gt<R>() * BAND_Q * CW;
     }
-    static __host__ __device__ constexpr int floats_fixed() { return (band_gb<R>() + band_gt<R>()) * BAND_Q * CW; }
+    static __host__ __device__ constexpr int floats_fixed()
+    {
+        return (band_gb<R>() + band_gt<R>()) * BAND_Q * CW + band_gt<R>() * BAND_KC * CW;
+    }
 };
 
 // Right-hand sides of dbyd2 for the rows [k0, k0 + n) of field column Fc (rows beyond n: 0),
@@ -109,7 +114,8 @@ __device__ __forceinline__ void band_publish(const BandDev &bd, const float *__r
 // the carries.
 template <int CW, int R>
 __device__ __forceinline__ void band_eval(const BandDev &bd, const float *__restrict__ uv, const BandCarry<CW, R> &cb,
-                                          int c, int g, int G, int k0, int n, int nz, const float *Rc, float (&x)[R])
+                                          int c, int g, int G, int k0, int n, int nz, const float *Rc, float (&x)[R],
+                                          bool thomas_top = false)
 {
     constexpr int KC = BAND_KC, Q = BAND_Q;
     float rhs[R];
@@ -156,7 +162,38 @@ __device__ __forceinline__ void band_eval(const BandDev &bd, const float *__rest
         }
     }
     const int o = nz - KC, gt0 = o / R;
-    if (k0 + n > o) {
+    if (k0 + n > o && thomas_top) {
+        // Top block by a direct tridiagonal solve: for ibc 1 and 2 the boundary row of T is not
+        // diagonally dominant and T^{-1} reaches 19 there, which a product with T^{-1} carries
+        // into FP32 rounding.  x at row o-1 (outside the corner block) from the band sums over
+        // 27 rows on either side, then the chunk-local Thomas sweeps over rows o .. nz-1.
+        const float *th = uv + 4 * KC * Q;
+        const int m0 = o - 1;
+        float lo = 0.f, up = 0.f;
+#pragma unroll
+        for (int d = 27; d >= 1; d--)
+            if (m0 - d >= 0) lo = fmaf(bd.rpow[d], Rc[(m0 - d) * CW + c], lo);
+#pragma unroll
+        for (int d = KC; d >= 1; d--) up = fmaf(bd.rpow[d], Rc[(m0 + d) * CW + c], up);
+        const float xm0 = bd.t0 * (Rc[m0 * CW + c] + lo + up);
+        float *y = cb.YT + (size_t)(g - gt0) * KC * CW + c;  // this group's column of the scratch
+        float prev = 0.f;
+        for (int m = 0; m < KC; m++) {
+            float v = Rc[(o + m) * CW + c];
+            if (m == 0) v = fmaf(-th[3 * KC], xm0, v);
+            v = v * __ldg(th + m);
+            if (m > 0) v = fmaf(-__ldg(th + KC + m), prev, v);
+            y[m * CW] = v;
+            prev = v;
+        }
+        for (int m = KC - 2; m >= 0; m--) {
+            prev = fmaf(-__ldg(th + 2 * KC + m + 1), prev, y[m * CW]);
+            y[m * CW] = prev;
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (r < n && k0 + r >= o) x[r] = y[(k0 + r - o) * CW];
+    } else if (k0 + n > o) {
         float s[Q];
 #pragma unroll
         for (int q = 0; q < Q; q++) {

@@ -185,7 +185,8 @@ bool build_ztab(int nz, int ibc, int nch, int L, HostZTab &t)
 struct HostBand {
     int nz = 0, q = 0;
     double t0 = 0, r = 0;
-    std::vector<double> uv;  // Ub [KC][Q], Vb [Q][KC], Ut [KC][Q], Vt [Q][KC]
+    std::vector<double> uv;  // Ub [KC][Q], Vb [Q][KC], Ut [KC][Q], Vt [Q][KC], then the top-block
+                             // Thomas factors ib [KC], lwib [KC], gm [KC] and the coupling lowr
     double err = 0;          // max |T^{-1} - band - corners| / max |T^{-1}|
 };
 
@@ -258,6 +259,22 @@ bool build_band(const HostZTab &tz, HostBand &h)
             dev = std::max(dev, std::fabs(Ti[(size_t)k * nz + j] - v));
         }
     h.err = dev / mx;
+    {  // Thomas factors of T restricted to the top KC rows (x[nz-KC-1] moves to the right-hand side)
+        std::vector<double> th((size_t)3 * KC + 1, 0.0);
+        double *ib = th.data(), *lwib = ib + KC, *gm = lwib + KC;
+        double bprev = 1.0;
+        ib[0] = 1.0;
+        for (int m = 1; m < KC; m++) {
+            const int k = o + m;
+            gm[m] = tz.uppr[k - 1] / bprev;
+            const double bet = 1.0 - tz.lowr[k] * gm[m];
+            ib[m] = 1.0 / bet;
+            lwib[m] = tz.lowr[k] * ib[m];
+            bprev = bet;
+        }
+        th[3 * KC] = tz.lowr[o];
+        h.uv.insert(h.uv.end(), th.begin(), th.end());
+    }
     return h.err < 1e-8;
 }
 
@@ -690,7 +707,11 @@ template <typename T>
 cudaError_t end_step(sparc_plan *p, const StepArgs<T> &a, cudaStream_t st)
 {
     Solver<T> &S = solver<T>(p);
-    if (a.ALO) return launch_end_step<T>(a, st);  // compensated (double-float) update
+    if (a.ALO) {  // compensated (double-float) update
+        if constexpr (sizeof(T) == 4)
+            if (p->cfg.nx % 16 == 0 && S.end_stream) return launch_end_step_comp(a, st);
+        return launch_end_step<T>(a, st);
+    }
     if (S.have_maps && p->cfg.column_impl == 1) return launch_end_step_tma<T>(S.maps, a, st);
     return S.end_stream ? launch_end_step_stream<T>(a, st) : launch_end_step<T>(a, st);
 }
@@ -1112,7 +1133,7 @@ int sparc_plan_describe(const sparc_plan_t *p, char *buf, int len)
                   ">";
         else if (S.have_maps && p->cfg.column_impl == 1) col = "col_stage_tma_kernel<float>";
         else col = "col_stage_kernel<float," + std::to_string(S.a.colw) + ">";
-        end = S.a.ALO ? "end_step_kernel<float>"
+        end = S.a.ALO ? (S.end_stream ? "end_step_comp_kernel" : "end_step_kernel<float>")
                       : (S.have_maps && p->cfg.column_impl == 1) ? "end_step_tma_kernel<float>"
                       : S.end_stream ? "end_step_stream_kernel<float>" : "end_step_kernel<float>";
     } else {

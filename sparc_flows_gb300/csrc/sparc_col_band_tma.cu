@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(BT_CW * 32, 2)
     // ---- 5: gradient of p, RHS v_z without advection; advection of v_x along z; v_z of stage s
     {
         float d[R];
-        band_eval<CW, R>(bd, bd.uv[1], C0, c, g, G, k0, n, nz, RA, d);
+        band_eval<CW, R>(bd, bd.uv[1], C0, c, g, G, k0, n, nz, RA, d, true);
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(BT_CW * 32, 2)
                 xz[m] = -Kri[k] * (gpz + xz[m]);
             }
         }
-        if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C1, c, g, G, k0, n, nz, RB, d);
+        if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C1, c, g, G, k0, n, nz, RB, d, true);
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(BT_CW * 32, 2)
     if (!bt_phase(bar, 4)) { bt_abort(bar, 5, a.d_err); return; }
     // ---- 7: finish RHS v_z (advection, source, boundary zeros)
     float d[R];
-    if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C0, c, g, G, k0, n, nz, RA, d);
+    if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C0, c, g, G, k0, n, nz, RA, d, true);
     float forcing = 0.f;
     const bool inject = (time <= a.src_until) && (time >= 0) && (time < a.ntab);
     if (inject && a.k_inj >= k0 && a.k_inj < k0 + n) {

@@ -415,6 +415,7 @@ template <typename T>
 cudaError_t launch_end_step_stream(const StepArgs<T> &a, cudaStream_t st);
 template <typename T>
 size_t end_stream_smem_bytes(int nz);
+cudaError_t launch_end_step_comp(const StepArgs<float> &a, cudaStream_t st);  // compensated (ALO) FP32
 
 struct ColMaps;
 template <int R>

@@ -91,6 +91,145 @@ __global__ void __launch_bounds__(END_CW *END_WARPS) end_step_stream_kernel(Step
     }
 }
 
+// ---- compensated variant (FP32 plans with low parts ALO): the state is carried as hi + lo
+// (~48 significant bits), a + deltat scr and FILTER_VARS_2D are evaluated in double-float
+// arithmetic (Knuth's TwoSum, FMA-exact products), so the 3600-step accumulation does not round
+// the state to FP32 every step.
+
+__device__ __forceinline__ void ef_two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void ef_add(float &hi, float &lo, float bh, float bl)  // (hi, lo) += (bh, bl)
+{
+    float s, e;
+    ef_two_sum(hi, bh, s, e);
+    e += lo + bl;
+    hi = s + e;
+    lo = e - (hi - s);
+}
+
+// h (x + y) for double-float x, y and an exactly representable h, added to (hi, lo).
+__device__ __forceinline__ void ef_axpy2(float &hi, float &lo, float h, float xh, float xl, float yh, float yl)
+{
+    float s, e;
+    ef_two_sum(xh, yh, s, e);
+    e += xl + yl;
+    const float p = h * s;
+    const float pe = fmaf(h, s, -p) + h * e;
+    ef_add(hi, lo, p, pe);
+}
+
+// The (xi, v) pair of one component in one block (xi's update reads the old v, which the same
+// block overwrites only after its barrier), 16 columns wide so that hi and lo of both fields
+// ([nz][16] each) leave room for two blocks per SM; thread (c, r) = column c, rows r, r + 32, ...
+constexpr int ENDC_CW = 16, ENDC_ROWS = 32;
+
+__device__ __forceinline__ void ef_filt11c(const float *H, const float *L, int k, int c, float &hi, float &lo)
+{
+    constexpr int W = ENDC_CW;
+    const float c0 = 0.75390625f, hs[5] = {0.205078125f, -0.1171875f, 0.0439453125f, -0.009765625f, 0.0009765625f};
+    hi = c0 * H[k * W + c];
+    lo = fmaf(c0, H[k * W + c], -hi) + c0 * L[k * W + c];
+#pragma unroll
+    for (int j = 1; j <= 5; j++)
+        ef_axpy2(hi, lo, hs[j - 1], H[(k - j) * W + c], L[(k - j) * W + c], H[(k + j) * W + c], L[(k + j) * W + c]);
+}
+
+__device__ __forceinline__ void ef_out(const float *H, const float *L, int k, int c, int nz, bool filt, float &hi,
+                                       float &lo)
+{
+    constexpr int W = ENDC_CW;
+    hi = H[k * W + c];
+    lo = L[k * W + c];
+    if (filt) {
+        if (k >= 5 && k <= nz - 6) {
+            ef_filt11c(H, L, k, c, hi, lo);
+        } else {
+            float h = 0.f, l = 0.f;
+            ef_axpy2(h, l, 0.5f, H[(k + 1) * W + c], L[(k + 1) * W + c], H[(k - 1) * W + c], L[(k - 1) * W + c]);
+            hi = h;
+            lo = l;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(ENDC_CW *ENDC_ROWS) end_step_comp_kernel(StepArgs<float> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_e[];
+    const int nz = a.nz, nx = a.nx;
+    float *Hxi = reinterpret_cast<float *>(smem_e), *Lxi = Hxi + (size_t)nz * ENDC_CW;
+    float *Hv = Lxi + (size_t)nz * ENDC_CW, *Lv = Hv + (size_t)nz * ENDC_CW;
+    const int c = threadIdx.x % ENDC_CW, r0 = threadIdx.x / ENDC_CW;
+    const int x = blockIdx.x * ENDC_CW + c;
+    const int p = blockIdx.y & 1, b = blockIdx.y >> 1;  // component (0: x, 1: z), solve
+    const size_t F = (size_t)nz * nx;
+    const int time = *a.d_time;
+    const int rec = (a.steps_out > 0) ? time / a.steps_out : 0;
+    const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec < a.nrec_cap && time >= 0;
+    float *snap = record && a.snaps ? a.snaps + ((size_t)b * a.nrec_cap + rec) * 6 * F : nullptr;
+    float *Axi = a.A + ((size_t)b * 4 + p) * F, *Av = a.A + ((size_t)b * 4 + 2 + p) * F;
+    float *Lxig = a.ALO + ((size_t)b * 4 + p) * F, *Lvg = a.ALO + ((size_t)b * 4 + 2 + p) * F;
+    const float *R4 = svp(a, a.slot_sm1, b, p), *R5 = svp(a, a.slot_s, b, p);
+    const float dt = a.dt, bs = a.bs;
+    const bool xbc = (x == 0 || x == nx - 1);
+
+#pragma unroll 2
+    for (int k = r0; k < nz; k += ENDC_ROWS) {
+        const size_t g = (size_t)k * nx + x;
+        const float v = __ldg(Av + g), r4 = __ldg(R4 + g), r5 = __ldg(R5 + g);
+        const float sxi = (k == 0 || xbc) ? 0.f : v + bs * r4;  // scr xi = v of stage 5, RHS zeros
+        float hx = __ldg(Axi + g), lx = __ldg(Lxig + g), hv = v, lv = __ldg(Lvg + g);
+        float d = dt * sxi;
+        ef_add(hx, lx, d, fmaf(dt, sxi, -d));
+        d = dt * r5;
+        ef_add(hv, lv, d, fmaf(dt, r5, -d));
+        Hxi[k * ENDC_CW + c] = hx;
+        Lxi[k * ENDC_CW + c] = lx;
+        Hv[k * ENDC_CW + c] = hv;
+        Lv[k * ENDC_CW + c] = lv;
+        if (snap) snap[(size_t)(4 + p) * F + g] = r5;
+        const int pi = pml_row(a, k);
+        if (pi >= 0) {  // pmlvars += deltat * scrpml (step.f90:112-115), component p
+            const size_t qz = (((size_t)b * 2 + p) * a.nzpml + pi) * nx + x;
+            a.PZ[qz] += dt * a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz];
+        }
+    }
+    __syncthreads();
+    const bool xf = a.filt_xall || ((x >= a.nh - 1) && (x <= nx - a.nh));
+    for (int k = r0; k < nz; k += ENDC_ROWS) {
+        const size_t g = (size_t)k * nx + x;
+        const bool filt = xf && k >= a.filt_k0 && k <= nz - 2;
+        float hx, lx, hv, lv;
+        ef_out(Hxi, Lxi, k, c, nz, filt, hx, lx);
+        ef_out(Hv, Lv, k, c, nz, filt, hv, lv);
+        Axi[g] = hx;
+        Lxig[g] = lx;
+        Av[g] = hv;
+        Lvg[g] = lv;
+        if (snap) {
+            snap[(size_t)p * F + g] = hx;
+            snap[(size_t)(2 + p) * F + g] = hv;
+        }
+        if (record && p == 1 && k == a.k_obs && a.seis) a.seis[((size_t)b * a.nrec_cap + rec) * nx + x] = hv;
+    }
+}
+
+cudaError_t launch_end_step_comp(const StepArgs<float> &a, cudaStream_t st)
+{
+    if (a.nx % ENDC_CW || !a.ALO) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)4 * a.nz * ENDC_CW * sizeof(float);
+    cudaError_t e =
+        cudaFuncSetAttribute(end_step_comp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(a.nx / ENDC_CW, 2 * a.nb);
+    end_step_comp_kernel<<<grid, ENDC_CW * ENDC_ROWS, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
 template <typename T>
 size_t end_stream_smem_bytes(int nz)
 {

@@ -184,6 +184,16 @@ def test_fp32_tracks_fp64(fp64_300, monkeypatch, impl, cw):
         assert rel_l2(st32[0, f], st64[0, f]) < 10 * FP32_TOL, f
 
 
+def test_fp32_plans_launch_the_banded_column_pass():
+    """FP32 plans of the standard grids run the geometric-band column pass (a silent fallback to
+    the partitioned solve would still pass the accuracy tests)."""
+    run, model, psi, cmul = make_case(nx=512, nsteps=10, length=400e8)
+    w = gpu_solver(run, model, psi, cmul, precision=32)
+    d = w.describe()
+    w.close()
+    assert d["column"].startswith("col_band_kernel<32,10,512,300>"), d
+
+
 def test_fp32_512_columns_track_fp64():
     """On 512-column grids FP32 row passes use the register-resident FFT (FP64 keeps the
     Stockham FFT): seismograms and state of 200 steps against FP64."""
