@@ -193,6 +193,76 @@ int sparc_zband_host(int nz, int ibc, const double *b, double *x, const double *
  * precomputed tables against dbyd2.f (dbyd2.f:8-235). */
 int sparc_zsolve_host(int nz, int ibc, int lmax, const double *b, double *x, const double *preset, int n1);
 
+/* ---------------------------------------------------------------------------------------------
+ * Gradient post-processing (replaces grad.py's array work, grad.py:42-117, 188-364).  Every
+ * array is FP64 on the device, x-fastest [nz][nx] as the kernels above; no call allocates: the
+ * caller passes a workspace of sparc_grad_workspace_bytes(nx, nz) bytes (the vector calls need
+ * sparc_grad_workspace_bytes(0, 0)).  Reductions are deterministic: fixed block count, fixed
+ * summation order, independent of the stream and of earlier calls.
+ * ------------------------------------------------------------------------------------------- */
+#define SPARC_SYM_NONE 0
+#define SPARC_SYM_SYM 1        /* symmetrize: 0.5 (a + a reversed in x) (grad.py:101) */
+#define SPARC_SYM_ASYM (-1)    /* antisymmetrize: 0.5 (a - a reversed in x) (grad.py:100) */
+#define SPARC_ZFILT_NONE 0
+#define SPARC_ZFILT_GAUSSIAN 1 /* scipy gaussian_filter1d along z, mode reflect, truncate 4 */
+#define SPARC_ZFILT_SMOOTH 2   /* grad.py's 11-point filter 'smooth' (grad.py:66-87), nz >= 11 */
+
+typedef struct {
+    int nx, nz;          /* grid; nx in the FFT table (64..1024, factors 2 and 3) */
+    int nsrc;            /* number of per-source kernels and hessians to sum */
+    double nk;           /* filterx width in wavenumbers (grad.py:111: 30) */
+    int sym;             /* SPARC_SYM_* (grad.py:112-115; main uses ASYM, grad.py:200) */
+    int zfilt;           /* SPARC_ZFILT_* (main: GAUSSIAN, grad.py:200) */
+    double zsigma;       /* Gaussian width in rows (grad.py:200: 2.0); radius int(4 sigma + 0.5) <= 32 */
+    double hess_floor;   /* floor of the normalised preconditioner (grad.py:196: 5e-3) */
+    int precondition;    /* 1: H as grad.py main forms it (below); 0: H = sum_s hessians[s] used
+                            as given, rho ignored (filter_and_symmetrize(totkern, hess),
+                            grad.py:109-117) */
+} sparc_grad_config_t;
+
+/* Workspace bytes for sparc_gradient on an nx x nz grid (and for the vector calls). */
+unsigned long long sparc_grad_workspace_bytes(int nx, int nz);
+
+/* The gradient of grad.py's main (grad.py:188-202, 109-117), precondition = 1:
+ *   K = sum_s kernels[s],  H = sum_s |hessians[s]| * rho[k],  H <- max(H / max H, hess_floor),
+ *   grad = zfilter(sym(filterx(K / H, nk))).
+ * kernels, hessians: [nsrc][nz][nx]; rho: [nz] device (column 3 of the model file);
+ * grad: [nz][nx]. */
+int sparc_gradient(const sparc_grad_config_t *cfg, const double *kernels, const double *hessians,
+                   const double *rho, double *grad, void *work, void *stream);
+
+/* *result (host) = sum_i a[i] * (b[i] - c[i]), or sum_i a[i] * b[i] when c is NULL.  Waits for
+ * the stream.  (np.sum(grad * (grad - lastgrad)), grad.py:227-233) */
+int sparc_vec_dot(long long n, const double *a, const double *b, const double *c, double *result,
+                  void *work, void *stream);
+
+/* y[i] = alpha * x[i] + beta * z[i] (z may be NULL: y = alpha x); y may alias x or z. */
+int sparc_vec_axpby(long long n, double alpha, const double *x, double beta, const double *z, double *y,
+                    void *stream);
+
+/* Update direction (grad.py:204-250).  algo 0: steepest descent, p = -g; 1: conjugate gradient,
+ * Polak-Ribiere (the reference's choice, grad.py:222-228), p = -g + beta p_prev with
+ * beta = g.(g - g_prev) / g_prev.g_prev; 2: Hestenes-Stiefel (grad.py:230-233),
+ * beta = g.(g - g_prev) / (g - g_prev).p_prev.  *beta (host, may be NULL) receives beta (0 for
+ * algo 0).  Waits for the stream for algo 1 and 2. */
+int sparc_update_direction(int algo, long long n, const double *g, const double *g_prev, const double *p_prev,
+                           double *p, double *beta, void *work, void *stream);
+
+/* L-BFGS direction p = -H g by the two-loop recursion over npairs (<= 64) pairs s[i] =
+ * m_{i+1} - m_i, y[i] = g_{i+1} - g_i, oldest first, H0 = (s.y / y.y) of the newest pair.
+ * s, y: HOST arrays of device pointers.  p must not alias g, s or y.  (grad.py:257-325 sets out
+ * to compute this with m = 4; its own code cannot run: np.dot with one argument.)  Waits for
+ * the stream. */
+int sparc_lbfgs_direction(long long n, int npairs, const double *const *s, const double *const *y,
+                          const double *g, double *p, void *work, void *stream);
+
+/* Line-search models (grad.py:351-364, kind 'linear'):
+ *   out[e][i] = model[i] + eps[e] * (update[i] / max(update)) * rms(model),
+ * max(update) signed and skipped when 0, rms(model) = sqrt(sum model^2 / n) replaced by 1 when
+ * 0.  eps: host [neps]; out: device [neps][n].  Waits for the stream. */
+int sparc_linesearch_models(long long n, const double *model, const double *update, int neps, const double *eps,
+                            double *out, void *work, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,7 +42,22 @@ SIGNATURES = {
     "sparc_kernels_accumulate_static": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_zband_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _dp]),
     "sparc_zsolve_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int]),
+    "sparc_grad_workspace_bytes": (ctypes.c_ulonglong, [ctypes.c_int, ctypes.c_int]),
+    "sparc_gradient": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "sparc_vec_dot": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _dp, _vp, _vp]),
+    "sparc_vec_axpby": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_double, _vp, ctypes.c_double, _vp, _vp, _vp]),
+    "sparc_update_direction": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong, _vp, _vp, _vp, _vp, _dp, _vp, _vp]),
+    "sparc_lbfgs_direction": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "sparc_linesearch_models": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, ctypes.c_int, _dp, _vp, _vp, _vp]),
 }
+
+
+class SparcGradConfig(ctypes.Structure):
+    """sparc_grad_config_t."""
+
+    _fields_ = [("nx", ctypes.c_int), ("nz", ctypes.c_int), ("nsrc", ctypes.c_int), ("nk", ctypes.c_double),
+                ("sym", ctypes.c_int), ("zfilt", ctypes.c_int), ("zsigma", ctypes.c_double),
+                ("hess_floor", ctypes.c_double), ("precondition", ctypes.c_int)]
 
 
 class SparcConfig(ctypes.Structure):

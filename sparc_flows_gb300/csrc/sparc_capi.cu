@@ -940,6 +940,12 @@ bool check_cfg(const sparc_config_t *c, std::string &why)
 // ===============================================================================================
 // C ABI
 // ===============================================================================================
+namespace sparc {
+// Error reporting for the entry points defined in other translation units (sparc_grad.cu):
+// the same per-thread message sparc_last_error returns.
+int report_error(int code, const std::string &msg) { return fail(code, msg); }
+}  // namespace sparc
+
 extern "C" {
 
 const char *sparc_last_error(void) { return g_err.c_str(); }

@@ -18,7 +18,7 @@ def header_functions():
     names = []
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
-        names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(sparc_\w+)\s*\(", text, flags=re.M)
+        names += re.findall(r"^\s*(?:const\s+)?(?:\w+\s+)*\w+\s*\*?\s*(sparc_\w+)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 
