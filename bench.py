@@ -179,6 +179,63 @@ def cpu_baseline_quick():
             "sample": f"{nsolve} FP64 forward solves x {steps} steps of the batch32 grid on {nsolve} host threads"}
 
 
+def gradient_stage(pipe, model, dev, reps=20, cpu=True):
+    """The gradient post-processing of grad.py on this batch's own kernels: sparc_gradient (kernel
+    sum, hessian preconditioning, x/z filters, antisymmetrisation), a conjugate-gradient direction
+    and three line-search models, timed with CUDA events; the oracle's NumPy restatement of
+    grad.py timed on the host beside it (grad.py is NumPy, so this is the reference's own
+    arithmetic cost, without its FITS reads)."""
+    import numpy as np
+    import torch
+
+    from sparc_flows_gb300 import gradient as GR
+
+    fk = pipe.final_kernels(summed=False)
+    kp, hs = fk["kernel_psi"].contiguous(), fk["hessian"].contiguous()
+    nsrc, nz, nx = kp.shape
+    rho = torch.as_tensor(np.ascontiguousarray(model[:, 2]), dtype=torch.float64, device=dev)
+    ws = GR.Workspace(nx, nz, dev)
+    stream = torch.cuda.current_stream()
+    g = GR.gradient_psi(kp, hs, rho, ws=ws)
+    gp, pp = 0.9 * g, -g
+    GR.update_direction("cg", g, gp, pp, ws=ws)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    for _ in range(reps):
+        GR.gradient_psi(kp, hs, rho, ws=ws)
+    ev[1].record(stream)
+    for _ in range(reps):
+        u, _ = GR.update_direction("cg", g, gp, pp, ws=ws)
+        GR.linesearch_models(g, u, [0.01, 0.02, 0.03], ws=ws)
+    ev[2].record(stream)
+    torch.cuda.synchronize()
+    grad_ms = ev[0].elapsed_time(ev[1]) / reps
+    upd_ms = ev[1].elapsed_time(ev[2]) / reps
+    n = nz * nx
+    grad_bytes = (2 * nsrc * n + n + nz) * 8  # per-source kernels and hessians read once, gradient written
+    peak, peak_kind = measured_peak_hbm()
+    out = {"workload": f"{nsrc} sources, nz={nz}, nx={nx}, FP64 (grad.py:188-202, 204-250, 351-378)",
+           "gradient_ms": grad_ms, "update_and_linesearch_ms": upd_ms,
+           "gradient_algorithmic_bytes": grad_bytes,
+           "gradient_achieved_gbs": grad_bytes / (grad_ms * 1e-3) / 1e9,
+           "gradient_frac_of_hbm": grad_bytes / (grad_ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+           "launches": {"gradient": 4, "cg_direction": 5, "linesearch_models": 5}}
+    if cpu:
+        from oracle import grad_oracle as go
+        kh, hh, gh = kp.cpu().numpy(), hs.cpu().numpy(), g.cpu().numpy()
+        t0 = time.perf_counter()
+        ref = go.gradient_psi(kh, hh, model[:, 2])
+        t1 = time.perf_counter()
+        uh, _ = go.cg_update(gh, 0.9 * gh, -gh)
+        go.ls_models(gh, uh, [0.01, 0.02, 0.03])
+        t2 = time.perf_counter()
+        out["cpu_numpy_ms"] = {"gradient": (t1 - t0) * 1e3, "update_and_linesearch": (t2 - t1) * 1e3,
+                               "cores": 1, "kind": "port"}
+        out["rel_err_vs_numpy"] = float(np.linalg.norm(gh - ref) / np.linalg.norm(ref))
+    return out
+
+
 # ----------------------------------------------------------------------------------------------
 def run_gpu(args):
     import numpy as np
@@ -323,6 +380,8 @@ def run_gpu(args):
             line["fp64_plain"] = plain
         if accuracy is not None:
             line["accuracy"] = accuracy
+        if not args.no_gradient:
+            line["gradient"] = gradient_stage(pipe, model, dev, cpu=not args.no_cpu)
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_quick()
         print(json.dumps(line), flush=True)
@@ -372,6 +431,73 @@ def run_uneven(args):
     ub.close()
 
 
+def run_3d(args):
+    """The 3-D configuration: 4 sources on a 256 x 256 x 300 grid (200 Mm box), axisymmetric
+    outflow, FP32.  One bench step = 100 time steps of the batch (the checkpoint interval);
+    value = grid-point steps / device time.  e2e: the same through WaveSolver3D with the source
+    table uploaded from the host and the v_z records read back every bench step."""
+    import numpy as np
+    import torch
+    from sparc_flows_gb300 import model as M
+    from sparc_flows_gb300.solver3d import WaveSolver3D
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    nx = ny = 256
+    nz, nsrc, chunk = 300, 4, 100
+    model, xl, v0, pats = M.workload_3d(nx, ny, nz, nsrc)
+    ws = WaveSolver3D(nx, ny, model, xl, nbatch=nsrc, precision=32, flows=True, steps_out=15,
+                      device=f"cuda:{local}")
+    ws.set_flow(*v0)
+    run = M.uneven_run(512, 3600)
+    amp = M.source_time_series(run, M.SourceSpec(0.0), 3600 + 8)[1:]
+    ws.set_source(pats, amp)
+    ws.reset(0)
+    for _ in range(args.warmup):
+        ws.forward(chunk)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            ws.forward(chunk)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    units = ws.point_steps(chunk) * args.steps
+    value = units / (ms * 1e-3)
+    # end to end: the source table from pinned host memory in, the records to pinned host memory out
+    amp_h = torch.as_tensor(amp).pin_memory()
+    rec_h = torch.empty((chunk // 15 + 1, nsrc, ny, nx), dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        ws.set_source(pats, amp_h.numpy())
+        rec = ws.forward(chunk)
+        rec_h[:rec.shape[0]].copy_(rec, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = units / args.steps * max(1, args.steps) / e2e_s
+    words = 15 * 6 + 10 + 5 * 3 + 15 * (2 * 20 / nz)  # 15 V + 10 + 5 B + 15 Naux/N, 20 PML levels: 117 words
+    peak, peak_kind = measured_peak_hbm()
+    achieved = words * 4 * value / 1e9
+    line = {"metric": "3-D grid-pt-steps/s (FP32 batched, option 16)", "value": value, "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "3d4: 4 sources, 256 x 256 x 300 polytrope, 200 Mm box, outflow 300 m/s, "
+                                   "100 time steps per bench step", "l2": "inputs larger than L2 (8 GB of fields)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_point_step": words * 4, "scope": "whole step"},
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": amp_h.numel() * 8,
+                    "d2h_bytes_per_step": int(rec_h.numel() * 4)},
+            "gpu_launches": None}
+    print(json.dumps(line), flush=True)
+    ws.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -382,11 +508,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain reference path")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy report")
-    ap.add_argument("--workload", default="batch32", choices=["batch32", "uneven48"],
+    ap.add_argument("--no-gradient", action="store_true", help="skip the gradient post-processing figures")
+    ap.add_argument("--workload", default="batch32", choices=["batch32", "uneven48", "3d4"],
                     help="uneven48: 48 solves of mixed grids, lengths and backgrounds (seed 0)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "3d4":
+        run_3d(args)
     elif args.workload == "uneven48":
         run_uneven(args)
     else:

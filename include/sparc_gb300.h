@@ -194,6 +194,65 @@ int sparc_zband_host(int nz, int ibc, const double *b, double *x, const double *
 int sparc_zsolve_host(int nz, int ibc, int lmax, const double *b, double *x, const double *preset, int n1);
 
 /* ---------------------------------------------------------------------------------------------
+ * 3-D solver: option 16, MP_FLOWS_PML_3D_DISPL (displacement.f90:377-477) with ddxyz
+ * (derivatives.f90:175-305), the 5-stage RK of STEP (step.f90:43-119) and
+ * FILTER_VARS_3D_HORIZ_PML after every step of odd index (physics.f90:836-882, step.f90:114).
+ * A batch of nbatch independent solves shares the background and the flow.  Device fields are
+ * [nz][nbatch][ny][nx] (level-major, x fastest); the state is six of them (xi_x, xi_y, xi_z,
+ * v_x, v_y, v_z), in the plan precision.  Laterally uniform background (profiles in z).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct sparc3d_plan sparc3d_plan_t;
+
+typedef struct {
+    int nx, ny, nz, nbatch;    /* nx in the FFT table and a multiple of 16; ny in 64..512 (2, 3) */
+    int precision;             /* 32 or 64 */
+    int npmlbot, npmltop;      /* vertical PML levels, each >= 5 (params.i:121) */
+    double deltat;             /* timestep*dimc/diml (initialize.f90:474) */
+    double stretchx, stretchy; /* rsun/xlength, rsun/ylength (initialize.f90:225-226) */
+    double betas[5];           /* RK coefficients times deltat (step.f90:34-40) */
+    int flows;                 /* 1: advection by v0 (v0 arrays required) */
+    int steps_out;             /* record cadence (driver.f90:388) */
+    int k_src;                 /* 0-based e_rad: source rows |k - e_rad| <= 4 (displacement.f90:456-462) */
+    int k_obs;                 /* 0-based o_rad: recorded level of v_z (driver.f90:391) */
+    int filter_every;          /* 2: FILTER_VARS_3D_HORIZ_PML after odd steps (HORIZONTAL_PMLS); 0: none */
+} sparc3d_config_t;
+
+/* FP64 device pointers, copied (and rounded for FP32 plans) into the plan.  Profiles are [nz]:
+ * stretch (initialize.f90:466-470), rhoinv, rho0, c2rho0 (physics.f90:204-205), gradp0_z,
+ * gradrho0_z and g with the PML decay factor applied (physics.f90:206-208, 263-286),
+ * source_dep (physics.f90:109); az, bz: [npmlbot + npmltop] (physics.f90:287-288);
+ * v0x, v0y, v0z: [nz][ny][nx] (NULL when flows == 0). */
+typedef struct {
+    const double *stretch, *rhoinv, *rho0, *c2rho0, *gradp0_z, *gradrho0_z, *g, *source_dep;
+    const double *az, *bz;
+    const double *v0x, *v0y, *v0z;
+} sparc3d_background_t;
+
+int sparc3d_plan_create(const sparc3d_config_t *cfg, sparc3d_plan_t **plan);
+int sparc3d_plan_destroy(sparc3d_plan_t *plan);
+int sparc3d_set_background(sparc3d_plan_t *plan, const sparc3d_background_t *bg, void *stream);
+
+/* Forcing of the RHS of v_z (displacement.f90:456-462): forcing(x, y) * source_dep(k) on rows
+ * |k - k_src| <= 4 with forcing = pattern[b][y][x] * amp[step] (0 past the table).  pattern:
+ * device FP64 [nbatch][ny][nx]; amp: host [namp].  (The reference assigns forcing only in
+ * LAGRANGE_INTERP, physics.f90:678-737: the caller supplies pattern * fwdsource for a forward
+ * run, as the 2-D routine injects vr * fwdsource, physics2d.f90:1056-1058.) */
+int sparc3d_set_source(sparc3d_plan_t *plan, const double *pattern, const double *amp, int namp, void *stream);
+
+/* Zero the state and PML auxiliaries; the next step has index time0. */
+int sparc3d_reset_state(sparc3d_plan_t *plan, int time0, void *stream);
+
+/* nsteps time steps (TIMESTEPPING, driver.f90:337-409).  After each step whose index is a
+ * multiple of steps_out, v_z at level k_obs ([nbatch][ny][nx]) is appended to seis (device,
+ * plan precision, room for nrec_cap records, may be NULL); *nrec (host, may be NULL) receives
+ * the number of records this call made. */
+int sparc3d_forward(sparc3d_plan_t *plan, int nsteps, void *seis, int nrec_cap, int *nrec, void *stream);
+
+/* State copy out / in: [6][nz][nbatch][ny][nx] of the plan precision (device). */
+int sparc3d_get_state(sparc3d_plan_t *plan, void *dst, void *stream);
+int sparc3d_set_state(sparc3d_plan_t *plan, const void *src, void *stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Gradient post-processing (replaces grad.py's array work, grad.py:42-117, 188-364).  Every
  * array is FP64 on the device, x-fastest [nz][nx] as the kernels above; no call allocates: the
  * caller passes a workspace of sparc_grad_workspace_bytes(nx, nz) bytes (the vector calls need

@@ -128,6 +128,24 @@ static void fft_exec(const orc_fft *f, double *re, double *im, double *tr, doubl
     }
 }
 
+/* Reusable plans for the 3-D restatement (sparc_oracle3d.c). */
+void *orc_fft_new(int n)
+{
+    orc_fft *f = (orc_fft *)calloc(1, sizeof(orc_fft));
+    if (!f || fft_plan(f, n)) { free(f); return NULL; }
+    return f;
+}
+void orc_fft_delete(void *f)
+{
+    if (!f) return;
+    fft_free((orc_fft *)f);
+    free(f);
+}
+void orc_fft_exec(const void *f, double *re, double *im, double *tr, double *ti, int sign)
+{
+    fft_exec((const orc_fft *)f, re, im, tr, ti, sign);
+}
+
 /* Public complex FFT for the tests (sign -1 forward / +1 inverse, unnormalised). */
 int orc_fft_c2c(int n, double *re, double *im, int sign)
 {

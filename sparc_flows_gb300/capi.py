@@ -42,6 +42,14 @@ SIGNATURES = {
     "sparc_kernels_accumulate_static": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_zband_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _dp]),
     "sparc_zsolve_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int]),
+    "sparc3d_plan_create": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "sparc3d_plan_destroy": (ctypes.c_int, [_vp]),
+    "sparc3d_set_background": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc3d_set_source": (ctypes.c_int, [_vp, _vp, _dp, ctypes.c_int, _vp]),
+    "sparc3d_reset_state": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "sparc3d_forward": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, _ip, _vp]),
+    "sparc3d_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc3d_set_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_grad_workspace_bytes": (ctypes.c_ulonglong, [ctypes.c_int, ctypes.c_int]),
     "sparc_gradient": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sparc_vec_dot": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _dp, _vp, _vp]),
@@ -50,6 +58,23 @@ SIGNATURES = {
     "sparc_lbfgs_direction": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sparc_linesearch_models": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, ctypes.c_int, _dp, _vp, _vp, _vp]),
 }
+
+
+class Sparc3DConfig(ctypes.Structure):
+    """sparc3d_config_t."""
+
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("nbatch", ctypes.c_int),
+                ("precision", ctypes.c_int), ("npmlbot", ctypes.c_int), ("npmltop", ctypes.c_int),
+                ("deltat", ctypes.c_double), ("stretchx", ctypes.c_double), ("stretchy", ctypes.c_double),
+                ("betas", ctypes.c_double * 5), ("flows", ctypes.c_int), ("steps_out", ctypes.c_int),
+                ("k_src", ctypes.c_int), ("k_obs", ctypes.c_int), ("filter_every", ctypes.c_int)]
+
+
+class Sparc3DBackground(ctypes.Structure):
+    """sparc3d_background_t (device pointers)."""
+
+    _fields_ = [(n, _vp) for n in ("stretch", "rhoinv", "rho0", "c2rho0", "gradp0_z", "gradrho0_z", "g",
+                                    "source_dep", "az", "bz", "v0x", "v0y", "v0z")]
 
 
 class SparcGradConfig(ctypes.Structure):

@@ -1302,3 +1302,348 @@ int sparc_zsolve_host(int nz, int ibc, int lmax, const double *b, double *x, con
 }
 
 }  // extern "C"
+
+// =============================================================================================
+// 3-D plans (option 16): buffers, one time step as a launch sequence, the C ABI.
+// =============================================================================================
+namespace {
+
+template <typename T>
+struct Plan3 {
+    std::vector<void *> allocs;
+    T *A = nullptr, *SCR = nullptr, *X = nullptr, *PV = nullptr, *SPV = nullptr, *PSI = nullptr;
+    T *D1 = nullptr, *D2 = nullptr, *D3 = nullptr, *PP = nullptr, *RHO = nullptr, *GX = nullptr, *GY = nullptr,
+      *GZ = nullptr;
+    T *prof = nullptr, *v0 = nullptr, *pat = nullptr;
+    DevZ<T> z[2];  // ibc 0, 1
+    DevFFT<T> fx, fy;
+    S3Bg<T> bg{};
+    const T *stretch = nullptr;
+};
+
+}  // namespace
+
+struct sparc3d_plan {
+    sparc3d_config_t cfg{};
+    int nch = 0, L = 0;
+    HostZTab hz[2];
+    Plan3<float> s32;
+    Plan3<double> s64;
+    std::vector<double> amp;
+    int time = 0;
+    bool have_bg = false;
+    long long F = 0, P = 0, nxy = 0;
+};
+
+namespace {
+
+template <typename T>
+Plan3<T> &plan3(sparc3d_plan *p);
+template <>
+Plan3<float> &plan3<float>(sparc3d_plan *p) { return p->s32; }
+template <>
+Plan3<double> &plan3<double>(sparc3d_plan *p) { return p->s64; }
+
+template <typename T>
+int alloc_plan3(sparc3d_plan *p)
+{
+    Plan3<T> &S = plan3<T>(p);
+    const sparc3d_config_t &c = p->cfg;
+    const long long F = p->F, P = p->P, nz = c.nz, npml = c.npmlbot + c.npmltop;
+    struct Req { T **ptr; size_t n; };
+    std::vector<Req> reqs = {
+        {&S.A, (size_t)6 * F}, {&S.SCR, (size_t)6 * F}, {&S.X, (size_t)6 * F},
+        {&S.PV, (size_t)2 * P}, {&S.SPV, (size_t)2 * P}, {&S.PSI, (size_t)2 * P},
+        {&S.D1, (size_t)F}, {&S.D2, (size_t)F}, {&S.D3, (size_t)F}, {&S.PP, (size_t)F}, {&S.RHO, (size_t)F},
+        {&S.GX, (size_t)F}, {&S.GY, (size_t)F}, {&S.GZ, (size_t)F},
+        {&S.prof, (size_t)(8 * nz + 2 * npml)}, {&S.v0, c.flows ? (size_t)3 * nz * p->nxy : 1},
+        {&S.pat, (size_t)c.nbatch * p->nxy},
+    };
+    for (auto &r : reqs) {
+        void *ptr = nullptr;
+        const size_t bytes = std::max<size_t>(r.n, 1) * sizeof(T);
+        cudaError_t e = cudaMalloc(&ptr, bytes);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        S.allocs.push_back(ptr);
+        e = cudaMemset(ptr, 0, bytes);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("cudaMemset: ") + cudaGetErrorString(e));
+        *r.ptr = (T *)ptr;
+    }
+    for (int ibc = 0; ibc < 2; ibc++) {
+        cudaError_t e = upload_ztab<T>(p->hz[ibc], S.z[ibc], S.allocs);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("table upload: ") + cudaGetErrorString(e));
+    }
+    cudaError_t e = upload_fft<T>(c.nx, S.fx, S.allocs);
+    if (e == cudaSuccess) e = upload_fft<T>(c.ny, S.fy, S.allocs);
+    if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("fft tables: ") + cudaGetErrorString(e));
+    T *q = S.prof;
+    S.stretch = q; q += nz;
+    S.bg.rhoinv = q; q += nz;
+    S.bg.rho0 = q; q += nz;
+    S.bg.c2rho0 = q; q += nz;
+    S.bg.gradp0_z = q; q += nz;
+    S.bg.gradrho0_z = q; q += nz;
+    S.bg.g = q; q += nz;
+    S.bg.source_dep = q; q += nz;
+    S.bg.az = q; q += npml;
+    S.bg.bz = q;
+    return SPARC_OK;
+}
+
+template <typename T>
+void free_plan3(Plan3<T> &S)
+{
+    for (void *q : S.allocs) cudaFree(q);
+    S.allocs.clear();
+}
+
+// ddxyz (derivatives.f90:175-305) pieces on fields [nz][nb][ny][nx]
+template <typename T>
+cudaError_t d3x(sparc3d_plan *p, const T *v, T *dv, cudaStream_t st)
+{
+    const Plan3<T> &S = plan3<T>(p);
+    const sparc3d_config_t &c = p->cfg;
+    return launch_ddx<T>(v, dv, c.nz * c.nbatch * c.ny, c.nx, (T)c.stretchx, S.fx.twr, S.fx.twi, S.fx.kap, st);
+}
+template <typename T>
+cudaError_t d3y(sparc3d_plan *p, const T *v, T *dv, cudaStream_t st)
+{
+    const Plan3<T> &S = plan3<T>(p);
+    const sparc3d_config_t &c = p->cfg;
+    return launch_ddy<T>(v, dv, c.nz * c.nbatch, c.nx, c.ny, (T)c.stretchy, S.fy.twr, S.fy.twi, S.fy.kap, st);
+}
+template <typename T>
+cudaError_t d3z(sparc3d_plan *p, const T *v, T *dv, int ibc, cudaStream_t st)
+{
+    const Plan3<T> &S = plan3<T>(p);
+    return launch_ddz<T>(S.z[ibc].tab, p->nch, p->L, v, dv, (int)(p->cfg.nbatch * p->nxy), p->cfg.nz, nullptr,
+                         S.stretch, 0, st);
+}
+
+// MP_FLOWS_PML_3D_DISPL (displacement.f90:377-477) on X (psi: PSI), into SCR and SPV.
+template <typename T>
+cudaError_t rhs3(sparc3d_plan *p, const T *X, const T *PSI, T amp, cudaStream_t st)
+{
+    Plan3<T> &S = plan3<T>(p);
+    const sparc3d_config_t &c = p->cfg;
+    const long long F = p->F, P = p->P;
+    const S3Args a{c.nx, c.ny, c.nz, c.nbatch, c.npmlbot, c.npmltop, c.k_src, c.flows, p->nxy};
+    cudaError_t e;
+#define R3(call) do { e = (call); if (e != cudaSuccess) return e; } while (0)
+    R3(d3x<T>(p, X, S.D1, st));
+    R3(d3y<T>(p, X + F, S.D2, st));
+    R3(d3z<T>(p, X + 2 * F, S.D3, 1, st));
+    R3(launch_s3_div<T>(a, S.bg, S.D1, S.D2, S.D3, X + 2 * F, PSI, S.SPV, S.PP, S.RHO, st));
+    R3(d3x<T>(p, S.PP, S.GX, st));
+    R3(d3y<T>(p, S.PP, S.GY, st));
+    R3(d3z<T>(p, S.PP, S.GZ, 0, st));
+    if (c.flows) {
+        const long long q = (long long)c.nz * p->nxy;
+        for (int comp = 0; comp < 3; comp++) {
+            const T *v = X + (3 + comp) * F;
+            R3(d3x<T>(p, v, S.D1, st));
+            R3(d3y<T>(p, v, S.D2, st));
+            R3(d3z<T>(p, v, S.D3, 1, st));
+            R3(launch_s3_adv<T>(a, S.D1, S.D2, S.D3, S.v0, S.v0 + q, S.v0 + 2 * q, S.SCR + (3 + comp) * F, st));
+        }
+    }
+    R3(launch_s3_rhs<T>(a, S.bg, X, S.SCR, S.GX, S.GY, S.GZ, PSI + P, S.SPV + P, S.RHO, S.pat, amp, st));
+#undef R3
+    return cudaSuccess;
+}
+
+// STEP (step.f90:43-119) and the record of TIMESTEPPING (driver.f90:388-409).
+template <typename T>
+cudaError_t step3(sparc3d_plan *p, T *seis, int cap, int &nrec, cudaStream_t st)
+{
+    Plan3<T> &S = plan3<T>(p);
+    const sparc3d_config_t &c = p->cfg;
+    const long long F = p->F, P = p->P;
+    const S3Args a{c.nx, c.ny, c.nz, c.nbatch, c.npmlbot, c.npmltop, c.k_src, c.flows, p->nxy};
+    const T amp = (T)(p->time >= 0 && p->time < (int)p->amp.size() ? p->amp[p->time] : 0.0);
+    cudaError_t e;
+    for (int s = 0; s < 5; s++) {
+        const T *X = S.A, *PSI = S.PV;
+        if (s > 0) {
+            e = launch_s3_stage_in<T>(6 * F, S.A, S.SCR, S.X, (T)c.betas[s], 2 * P, S.PV, S.SPV, S.PSI, st);
+            if (e != cudaSuccess) return e;
+            X = S.X;
+            PSI = S.PSI;
+        }
+        e = rhs3<T>(p, X, PSI, amp, st);
+        if (e != cudaSuccess) return e;
+    }
+    const int filter = (c.filter_every == 2 && (p->time + 1) % 2 == 0) ? 1 : 0;
+    e = launch_s3_end<T>(a, S.A, S.SCR, (T)c.deltat, filter, S.PV, S.SPV, st);
+    if (e != cudaSuccess) return e;
+    if (c.steps_out > 0 && p->time % c.steps_out == 0) {
+        if (seis && nrec < cap) {
+            const size_t lvl = (size_t)c.nbatch * p->nxy;
+            e = cudaMemcpyAsync(seis + (size_t)nrec * lvl, S.A + 5 * F + (size_t)c.k_obs * lvl, lvl * sizeof(T),
+                                cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+        nrec++;
+    }
+    p->time++;
+    return cudaSuccess;
+}
+
+bool check_cfg3(const sparc3d_config_t *c, std::string &why)
+{
+    if (c->precision != 32 && c->precision != 64) { why = "precision must be 32 or 64"; return false; }
+    if (c->nbatch < 1) { why = "nbatch must be >= 1"; return false; }
+    if (!fft_size_supported(c->nx) || c->nx % 16) { why = "nx not in the FFT table or not a multiple of 16"; return false; }
+    if (!ddy_size_supported(c->ny)) { why = "ny not in 64, 128, 192, 256, 384, 512"; return false; }
+    if (c->precision == 64 && c->ny > 384) { why = "ny > 384 needs more shared memory than a block has in FP64"; return false; }
+    if (c->npmlbot < 5 || c->npmltop < 5) { why = "npmlbot and npmltop must be >= 5 (filter window)"; return false; }
+    if (c->nz < c->npmlbot + c->npmltop + 1 || c->nz < 11) { why = "nz too small for the PML layers"; return false; }
+    if (c->k_src < 0 || c->k_src >= c->nz || c->k_obs < 0 || c->k_obs >= c->nz) { why = "k_src / k_obs out of range"; return false; }
+    if (c->filter_every != 0 && c->filter_every != 2) { why = "filter_every must be 0 or 2"; return false; }
+    if ((long long)c->nz * c->nbatch * c->ny > 2147483647LL || (long long)c->nz * c->nbatch > 65535) {
+        why = "nz * nbatch * ny (x-pass rows) or nz * nbatch (y-pass planes) too large";
+        return false;
+    }
+    return true;
+}
+
+template <typename T>
+int set_bg3(sparc3d_plan *p, const sparc3d_background_t *bg, cudaStream_t st)
+{
+    Plan3<T> &S = plan3<T>(p);
+    const sparc3d_config_t &c = p->cfg;
+    const int nz = c.nz, npml = c.npmlbot + c.npmltop;
+    const double *prof[8] = {bg->stretch, bg->rhoinv, bg->rho0, bg->c2rho0, bg->gradp0_z, bg->gradrho0_z, bg->g,
+                             bg->source_dep};
+    for (int i = 0; i < 8; i++) CK(cast_to<T>(prof[i], S.prof + (size_t)i * nz, nz, st));
+    CK(cast_to<T>(bg->az, S.prof + (size_t)8 * nz, npml, st));
+    CK(cast_to<T>(bg->bz, S.prof + (size_t)8 * nz + npml, npml, st));
+    if (c.flows) {
+        const size_t q = (size_t)nz * p->nxy;
+        CK(cast_to<T>(bg->v0x, S.v0, q, st));
+        CK(cast_to<T>(bg->v0y, S.v0 + q, q, st));
+        CK(cast_to<T>(bg->v0z, S.v0 + 2 * q, q, st));
+    }
+    return SPARC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sparc3d_plan_create(const sparc3d_config_t *cfg, sparc3d_plan_t **out)
+{
+    if (!cfg || !out) return fail(SPARC_ERR_ARG, "sparc3d_plan_create: null argument");
+    *out = nullptr;
+    std::string why;
+    if (!check_cfg3(cfg, why)) return fail(SPARC_ERR_SIZE, "sparc3d_plan_create: " + why);
+    sparc3d_plan *p = new sparc3d_plan();
+    p->cfg = *cfg;
+    p->nxy = (long long)cfg->nx * cfg->ny;
+    p->F = p->nxy * cfg->nbatch * cfg->nz;
+    p->P = p->nxy * cfg->nbatch * (cfg->npmlbot + cfg->npmltop);
+    if (!chunking(cfg->nz, 16, p->nch, p->L)) {
+        delete p;
+        return fail(SPARC_ERR_SIZE, "sparc3d_plan_create: nz too large for the column chunking");
+    }
+    for (int ibc = 0; ibc < 2; ibc++)
+        if (!build_ztab(cfg->nz, ibc, p->nch, p->L, p->hz[ibc])) {
+            delete p;
+            return fail(SPARC_ERR_SIZE, "sparc3d_plan_create: singular reduced system");
+        }
+    const int rc = cfg->precision == 32 ? alloc_plan3<float>(p) : alloc_plan3<double>(p);
+    if (rc != SPARC_OK) {
+        std::string m = g_err;
+        sparc3d_plan_destroy(p);
+        return fail(rc, m);
+    }
+    *out = p;
+    return SPARC_OK;
+}
+
+int sparc3d_plan_destroy(sparc3d_plan_t *p)
+{
+    if (!p) return SPARC_OK;
+    free_plan3(p->s32);
+    free_plan3(p->s64);
+    delete p;
+    return SPARC_OK;
+}
+
+int sparc3d_set_background(sparc3d_plan_t *p, const sparc3d_background_t *bg, void *stream)
+{
+    if (!p || !bg) return fail(SPARC_ERR_ARG, "sparc3d_set_background: null argument");
+    const double *need[10] = {bg->stretch, bg->rhoinv, bg->rho0, bg->c2rho0, bg->gradp0_z, bg->gradrho0_z, bg->g,
+                              bg->source_dep, bg->az, bg->bz};
+    for (const double *q : need)
+        if (!q) return fail(SPARC_ERR_ARG, "sparc3d_set_background: missing profile");
+    if (p->cfg.flows && (!bg->v0x || !bg->v0y || !bg->v0z))
+        return fail(SPARC_ERR_ARG, "sparc3d_set_background: flows on but v0 missing");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int rc = p->cfg.precision == 32 ? set_bg3<float>(p, bg, st) : set_bg3<double>(p, bg, st);
+    if (rc == SPARC_OK) p->have_bg = true;
+    return rc;
+}
+
+int sparc3d_set_source(sparc3d_plan_t *p, const double *pattern, const double *amp, int namp, void *stream)
+{
+    if (!p || !pattern || namp < 0 || (namp > 0 && !amp)) return fail(SPARC_ERR_ARG, "sparc3d_set_source: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t n = (size_t)p->cfg.nbatch * p->nxy;
+    if (p->cfg.precision == 32) CK(cast_to<float>(pattern, p->s32.pat, n, st));
+    else CK(cast_to<double>(pattern, p->s64.pat, n, st));
+    p->amp.assign(amp, amp + namp);
+    return SPARC_OK;
+}
+
+int sparc3d_reset_state(sparc3d_plan_t *p, int time0, void *stream)
+{
+    if (!p) return fail(SPARC_ERR_ARG, "sparc3d_reset_state: null plan");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
+    void *A = p->cfg.precision == 32 ? (void *)p->s32.A : (void *)p->s64.A;
+    void *SCR = p->cfg.precision == 32 ? (void *)p->s32.SCR : (void *)p->s64.SCR;
+    void *PV = p->cfg.precision == 32 ? (void *)p->s32.PV : (void *)p->s64.PV;
+    void *SPV = p->cfg.precision == 32 ? (void *)p->s32.SPV : (void *)p->s64.SPV;
+    CK(cudaMemsetAsync(A, 0, 6 * p->F * es, st));
+    CK(cudaMemsetAsync(SCR, 0, 6 * p->F * es, st));
+    CK(cudaMemsetAsync(PV, 0, 2 * p->P * es, st));
+    CK(cudaMemsetAsync(SPV, 0, 2 * p->P * es, st));
+    p->time = time0;
+    return SPARC_OK;
+}
+
+int sparc3d_forward(sparc3d_plan_t *p, int nsteps, void *seis, int nrec_cap, int *nrec, void *stream)
+{
+    if (!p || nsteps < 0 || nrec_cap < 0) return fail(SPARC_ERR_ARG, "sparc3d_forward: bad argument");
+    if (!p->have_bg) return fail(SPARC_ERR_STATE, "sparc3d_forward: background not set");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int n = 0;
+    for (int i = 0; i < nsteps; i++) {
+        cudaError_t e = p->cfg.precision == 32 ? step3<float>(p, (float *)seis, nrec_cap, n, st)
+                                               : step3<double>(p, (double *)seis, nrec_cap, n, st);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("sparc3d_forward: ") + cudaGetErrorString(e));
+    }
+    if (nrec) *nrec = n;
+    return SPARC_OK;
+}
+
+int sparc3d_get_state(sparc3d_plan_t *p, void *dst, void *stream)
+{
+    if (!p || !dst) return fail(SPARC_ERR_ARG, "sparc3d_get_state: null argument");
+    const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
+    const void *A = p->cfg.precision == 32 ? (const void *)p->s32.A : (const void *)p->s64.A;
+    CK(cudaMemcpyAsync(dst, A, 6 * p->F * es, cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
+    return SPARC_OK;
+}
+
+int sparc3d_set_state(sparc3d_plan_t *p, const void *src, void *stream)
+{
+    if (!p || !src) return fail(SPARC_ERR_ARG, "sparc3d_set_state: null argument");
+    const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
+    void *A = p->cfg.precision == 32 ? (void *)p->s32.A : (void *)p->s64.A;
+    CK(cudaMemcpyAsync(A, src, 6 * p->F * es, cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
+    return SPARC_OK;
+}
+
+}  // extern "C"

@@ -405,6 +405,36 @@ cudaError_t launch_kacc(const KAccArgs<T> &k, cudaStream_t st);
 
 bool fft_size_supported(int n);
 
+// ------------------------------------------------------------------------------------------
+// 3-D displacement step (sparc_3d.cu).  Fields [nz][nb][ny][nx]; nxy = nx * ny.
+struct S3Args {
+    int nx, ny, nz, nb, npmlbot, npmltop, e_rad, flows;
+    long long nxy;
+};
+template <typename T>
+struct S3Bg {  // profiles in z ([nz]) and PML coefficients ([npmlbot + npmltop])
+    const T *rhoinv, *rho0, *c2rho0, *gradp0_z, *gradrho0_z, *g, *source_dep, *az, *bz;
+};
+bool ddy_size_supported(int ny);
+template <typename T>
+cudaError_t launch_ddy(const T *var, T *dvar, int nplanes, int nx, int ny, T stretchy, const T *twr, const T *twi,
+                       const T *kap, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s3_stage_in(long long n6, const T *A, const T *SCR, T *X, T beta, long long np, const T *PV,
+                               const T *SPV, T *PSI, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s3_div(const S3Args &a, const S3Bg<T> &bg, const T *D1, const T *D2, T *D3, const T *XIZ,
+                          const T *PSIVZ, T *SPSIVZ, T *PP, T *RHO, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s3_adv(const S3Args &a, const T *D1, const T *D2, const T *D3, const T *V0X, const T *V0Y,
+                          const T *V0Z, T *OUT, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s3_rhs(const S3Args &a, const S3Bg<T> &bg, const T *X, T *SCR, const T *GX, const T *GY,
+                          const T *GZ, const T *PSIP, T *SPSIP, const T *RHO, const T *PAT, T amp, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s3_end(const S3Args &a, T *A, const T *SCR, T dt, int filter, T *PV, const T *SPV,
+                          cudaStream_t st);
+
 template <int CW, int R>
 cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st);
 size_t col_band_smem_bytes(int nz, int R, int cw);

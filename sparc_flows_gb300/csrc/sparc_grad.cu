@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(GRAD_THREADS) grad_sum_kernel(const double *__
     double m = 0.0;
     for (long long i = (long long)blockIdx.x * GRAD_THREADS + threadIdx.x; i < n; i += (long long)GRAD_BLOCKS * GRAD_THREADS) {
         double ks = 0.0, hs = 0.0;
-        for (int s = 0; s < nsrc; s++) {
+#pragma unroll 8
+        for (int s = 0; s < nsrc; s++) {  // unrolled so that eight sources' loads are in flight
             ks += kern[(size_t)s * n + i];
             const double h = hess[(size_t)s * n + i];
             hs += precondition ? fabs(h) : h;

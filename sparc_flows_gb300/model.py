@@ -248,3 +248,69 @@ def uneven_solves(n: int = 48, seed: int = 0) -> list[Solve]:
 def uneven_run(nx: int, nsteps: int) -> RunConfig:
     """Run configuration of one group of the uneven batch (batch32 physics, 20-layer bottom PML)."""
     return RunConfig(nx=nx, nz=300, xlength_cm=nx * 0.78125e8, nsteps=nsteps, flows=True, npmlbot=20)
+
+
+# ---------------------------------------------------------------------------------------------
+# 3-D configuration (256 x 256 x 300, 200 Mm box, 4 sources, axisymmetric outflow): synthetic
+# inputs for the option-16 solver (solver3d.py).
+# ---------------------------------------------------------------------------------------------
+def outflow_3d(nx: int, ny: int, model: np.ndarray, xlength_cm: float, u0_ms: float = 300.0,
+               sigma_mm: float = 10.0, zc_mm: float = -2.0, zw_mm: float = 2.0, zret_mm: float = -6.0,
+               zwret_mm: float = 3.0):
+    """Axisymmetric outflow u_r(r, z) = u0 (r/sigma) exp(1/2 - r^2/(2 sigma^2)) f(z) about the box
+    centre, f(z) = exp(-((z-zc)/zw)^2) - a exp(-((z-zret)/zwret)^2), with v_z from
+    d(rho0 v_z)/dz = -rho0 div_h(u) integrated upward from the bottom (trapezoid rule in z,
+    spectral horizontal divergence).  The deeper return flow (a set so that the integral of
+    rho0 f vanishes) closes the mass flux of each column: without it v_z = flux / rho0 grows to
+    ~190 km/s where rho0 falls off at the top.  Returns (v0x, v0y, v0z), each (nz, ny, nx),
+    nondimensional (cm/s / dimc)."""
+    L = xlength_cm * 1e-8
+    x = (np.arange(nx) / nx - 0.5) * L
+    y = (np.arange(ny) / ny - 0.5) * L
+    X, Y = np.meshgrid(x, y)  # (ny, nx), Mm
+    r = np.sqrt(X * X + Y * Y)
+    z = z_mm(model)
+    rho = model[:, 2]
+    zc = z * 1e8  # cm
+    f1 = np.exp(-((z - zc_mm) / zw_mm) ** 2)
+    f2 = np.exp(-((z - zret_mm) / zwret_mm) ** 2)
+    w = np.gradient(zc)
+    prof = f1 - (np.sum(rho * f1 * w) / np.sum(rho * f2 * w)) * f2
+    ur = u0_ms * 100.0 * (r / sigma_mm) * np.exp(0.5 - r * r / (2 * sigma_mm ** 2))  # cm/s
+    with np.errstate(invalid="ignore", divide="ignore"):
+        cx = np.where(r > 0, X / r, 0.0)
+        cy = np.where(r > 0, Y / r, 0.0)
+    ux = (ur * cx)[None] * prof[:, None, None]
+    uy = (ur * cy)[None] * prof[:, None, None]
+    kx = 2 * np.pi * np.fft.fftfreq(nx, d=L * 1e8 / nx)
+    ky = 2 * np.pi * np.fft.fftfreq(ny, d=L * 1e8 / ny)
+    divh = (np.fft.ifft(1j * kx[None, None, :] * np.fft.fft(ux, axis=2), axis=2).real
+            + np.fft.ifft(1j * ky[None, :, None] * np.fft.fft(uy, axis=1), axis=1).real)  # 1/s
+    flux = np.zeros_like(divh)
+    src = -rho[:, None, None] * divh
+    for k in range(1, len(z)):
+        flux[k] = flux[k - 1] + 0.5 * (src[k] + src[k - 1]) * (zc[k] - zc[k - 1])
+    uz = flux / rho[:, None, None]
+    return ux / DIMC, uy / DIMC, uz / DIMC
+
+
+def point_source_pattern(nx: int, ny: int, xlength_cm: float, xs_mm: float, ys_mm: float) -> np.ndarray:
+    """Radial form of the reference's source profile exp(-d^2/(400 dx^2)) sinc(0.43 pi d)
+    (driver.f90:541-547) about (xs, ys), d the horizontal distance in Mm: (ny, nx)."""
+    L = xlength_cm * 1e-8
+    x = (np.arange(nx) / nx - 0.5) * L
+    y = (np.arange(ny) / ny - 0.5) * L
+    X, Y = np.meshgrid(x, y)
+    d = np.sqrt((X - xs_mm) ** 2 + (Y - ys_mm) ** 2)
+    dx = L / nx
+    return np.exp(-d * d / (400.0 * dx * dx)) * np.sinc(0.43 * d)
+
+
+def workload_3d(nx: int = 256, ny: int = 256, nz: int = 300, nsrc: int = 4):
+    """The 3-D configuration: polytrope, 200 Mm box, outflow, sources at (+-50, +-50) Mm."""
+    model = polytrope(nz)
+    xl = 200e8
+    v0 = outflow_3d(nx, ny, model, xl)
+    pos = [(-50.0, -50.0), (50.0, -50.0), (-50.0, 50.0), (50.0, 50.0)][:nsrc]
+    pats = np.stack([point_source_pattern(nx, ny, xl, xs, ys) for xs, ys in pos])
+    return model, xl, v0, pats
