@@ -253,6 +253,35 @@ int sparc3d_get_state(sparc3d_plan_t *plan, void *dst, void *stream);
 int sparc3d_set_state(sparc3d_plan_t *plan, const void *src, void *stream);
 
 /* ---------------------------------------------------------------------------------------------
+ * Travel-time adjoint source (ADJOINT_SOURCE_FILT, driver.f90:1758-2238), FP64, for a batch of
+ * sources.  Records are [nbatch][nt][nx] (x fastest; nt records of vz at o_rad), device.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct sparc_tt_plan sparc_tt_plan_t;
+
+/* nx in the FFT table; nt (records) in 2..860; max_rows: most receivers measured by one mode
+ * call over the batch. */
+int sparc_tt_plan_create(int nx, int nt, int nbatch, int max_rows, sparc_tt_plan_t **plan);
+int sparc_tt_plan_destroy(sparc_tt_plan_t *plan);
+
+/* Forward (x, t) transforms of the synthetic and observed records (driver.f90:1838-1844) and a
+ * zero adjoint source. */
+int sparc_tt_set_records(sparc_tt_plan_t *plan, const double *synth, const double *data, void *stream);
+
+/* One ridge filter ("mode", driver.f90:1948-2113): filter [nt][nx] device, real (the ridge times
+ * its frequency filter).  rows: host [nrows][7] = source b, receiver x (0-based), search range
+ * timest, timefin (1-based, clipped to the record), lef, rig (1-based window: in when given,
+ * out otherwise), loc (out: the picked maximum); halftime = nint(window / (2 dt)); dt_min = the
+ * record cadence in minutes.  tau: host [nrows] out, travel-time shifts in minutes (COMPUTE_TT_
+ * GIZONBIRCH, driver.f90:894-940).  The mode's contribution is added, time-reversed, to the
+ * adjoint source.  Waits for the stream. */
+int sparc_tt_mode(sparc_tt_plan_t *plan, const double *filter, int nrows, int *rows, int halftime, int given,
+                  double dt_min, double *tau, void *stream);
+
+/* The adjoint source of every source, [nbatch][nt][nx] device, times nt / 60 (driver.f90:2201),
+ * in the reference's time-reversed order (ready for source.fits). */
+int sparc_tt_adjoint(sparc_tt_plan_t *plan, double *adj, void *stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Gradient post-processing (replaces grad.py's array work, grad.py:42-117, 188-364).  Every
  * array is FP64 on the device, x-fastest [nz][nx] as the kernels above; no call allocates: the
  * caller passes a workspace of sparc_grad_workspace_bytes(nx, nz) bytes (the vector calls need

@@ -50,6 +50,13 @@ SIGNATURES = {
     "sparc3d_forward": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, _ip, _vp]),
     "sparc3d_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc3d_set_state": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc_tt_plan_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(_vp)]),
+    "sparc_tt_plan_destroy": (ctypes.c_int, [_vp]),
+    "sparc_tt_set_records": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "sparc_tt_mode": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp,
+                                     _vp]),
+    "sparc_tt_adjoint": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_grad_workspace_bytes": (ctypes.c_ulonglong, [ctypes.c_int, ctypes.c_int]),
     "sparc_gradient": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sparc_vec_dot": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _dp, _vp, _vp]),

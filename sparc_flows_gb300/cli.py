@@ -18,11 +18,15 @@ The partial states the reference dumps every 15 steps as ~3000 FITS files
 (all_modules.f90:750-784) are kept as one array file per run (partial_states.npy) in the same
 folders and removed by the kernel stage, as PRODUCE_KERNELS removes its *partial* files.
 
-Adjoint source: the travel-time adjoint source of ADJOINT_SOURCE_FILT (driver.f90:1758-2238) is
-not part of this build; a forward run that is not a data run writes a waveform adjoint source
-(time-reversed synthetic minus <dir>/data/NN.fits at every column) to adjoint_srcNN/source.fits.
+Adjoint source: a forward run that is not a data run computes the travel-time adjoint source
+of ADJOINT_SOURCE_FILT (driver.f90:1758-2238; ttadjoint.py, csrc/sparc_tt.cu) from the ridge
+filters selected by <dir>/params.<pord> and <dir>/filter.params.* and writes
+adjoint_srcNN/{source.fits, information}, forward_srcNN_lsMM/ttdiff.<pord>,
+forward_srcNN_ls00/windows.<pord> and kernel/misfit_NN_MM; SPARC_ADJOINT_SOURCE=waveform
+writes the time-reversed waveform residual (synthetic minus <dir>/data/NN.fits) instead.
 
-Environment: SPARC_PRECISION (64, or 32), SPARC_DEVICE (cuda:0), SPARC_NSTEPS (override maxtime+1).
+Environment: SPARC_PRECISION (64, or 32), SPARC_DEVICE (cuda:0), SPARC_NSTEPS (override maxtime+1),
+SPARC_ADJOINT_SOURCE (tt, or waveform).
 """
 from __future__ import annotations
 
@@ -133,12 +137,33 @@ def _forward(run, model, directory, contrib, jobno, src, precision, device, comp
         np.save(os.path.join(out, "partial_states.npy"), snaps.cpu().numpy()[0])
     if not compute_data:
         data_p = os.path.join(directory, "data", f"{contrib}.fits")
-        adir = os.path.join(directory, f"adjoint_src{contrib}")
-        os.makedirs(adir, exist_ok=True)
         data = fits.read(data_p).reshape(s.shape) if os.path.exists(data_p) else np.zeros_like(s)
-        fits.write(os.path.join(adir, "source.fits"), (s - data)[::-1][:, None, :])
+        if os.environ.get("SPARC_ADJOINT_SOURCE", "tt") == "waveform":
+            adir = os.path.join(directory, f"adjoint_src{contrib}")
+            os.makedirs(adir, exist_ok=True)
+            fits.write(os.path.join(adir, "source.fits"), (s - data)[::-1][:, None, :])
+        else:
+            _tt_adjoint(run, directory, contrib, jobno, xloc, s, data, device)
     ws.close()
     return 0
+
+
+def _tt_adjoint(run, directory, contrib, jobno, xloc, synth, data, device):
+    """ADJOINT_SOURCE_FILT (driver.f90:1758-2238) after a forward run that is not a data run:
+    travel times of the ridge-filtered records, adjoint source, misfit files."""
+    import torch
+
+    from .ttadjoint import TTAdjoint, read_measurement_files, read_windows, write_outputs
+
+    linesearch = os.path.exists("linesearch")
+    tl = np.loadtxt(os.path.join(directory, f"forward_src{contrib}_ls{jobno}", "timeline"), ndmin=2)[:, 1]
+    t_min = -tl[::-1] / 60.0
+    modes, freq = read_measurement_files(directory)
+    windows = read_windows(directory, contrib, modes) if linesearch else None
+    tt = TTAdjoint(run.nx, synth.shape[0], 1, run.xlength_cm, float(run.outputcad), device=device)
+    res = tt.run(torch.as_tensor(synth[None]), torch.as_tensor(data[None]), [xloc], t_min, modes, freq, windows)
+    write_outputs(directory, contrib, jobno, res, 0, t_min, linesearch, os.path.exists("compute_synth"))
+    tt.close()
 
 
 def _adjoint(run, model, directory, contrib, jobno, precision, device):

@@ -1,0 +1,493 @@
+// sparc_tt.cu -- travel-time adjoint source on the device (ADJOINT_SOURCE_FILT,
+// driver.f90:1758-2238), FP64, for a batch of sources.
+//
+// The reference, per ridge filter ("mode") and per measured receiver i, windows the time
+// derivative of the filtered synthetic at x_i, transforms it, multiplies by the filter and by
+// exp(-i k x_i), transforms the whole (x, t) plane back and adds the result, scaled by
+// -tau_i / (sum ccdot^2 dt), time-reversed into the adjoint source: one 2-D transform per
+// receiver.  The sum over receivers is linear, and exp(-2 pi i k (i-1)/nx) is the forward DFT
+// kernel of a point at x_i, so it equals one transform per mode:
+//     adj_mode = Re IDFT2( filter * DFT2(c) ),  c(x_i, t) = con_i w_i(t) ccdot(x_i, t),
+// with c zero at unmeasured x.  Per mode and batch: three inverse 2-D transforms (filtered
+// synthetic, filtered data, time derivative), the Gizon-Birch derivative of the synthetic along
+// t, per-receiver reductions (window pick, travel time, normalisation), and one forward plus
+// one inverse 2-D transform of c.
+//
+// Fields are complex [nb][nt][nx] (x fastest).  x transforms: one warp per row, the shared-
+// memory Stockham FFT of the wave solver (nx in its table).  t transforms: any nt, direct DFT
+// over a 16-column tile held in shared memory (nt^2 nx operations per transform; nt is the
+// number of records, a few hundred).  FFTW's transforms are unnormalised, and so are these.
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "sparc_common.cuh"
+#include "sparc_gb300.h"
+
+namespace sparc {
+int report_error(int code, const std::string &msg);
+}
+using namespace sparc;
+
+namespace {
+
+constexpr int TT_THREADS = 256;
+constexpr int TT_COLS = 16;      // columns per block of the t transform
+constexpr int TT_XWPB = 2;       // rows (warps) per block of the x transform
+constexpr double TT_PI = 3.141592653589793;
+
+// x transform of complex rows in place, sign -1 forward, +1 inverse (unnormalised).
+template <int N>
+__global__ void __launch_bounds__(TT_XWPB *WARP) tt_fft_x_kernel(double2 *data, long long nrows, const double *twr,
+                                                                 const double *twi, int inverse)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *sm = reinterpret_cast<double *>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long row = (long long)blockIdx.x * TT_XWPB + warp;
+    if (row >= nrows) return;
+    double *xr = sm + (size_t)warp * 4 * N, *xi = xr + N, *yr = xi + N, *yi = yr + N;
+    double2 *d = data + row * N;
+    for (int x = lane; x < N; x += WARP) {
+        const double2 v = d[x];
+        xr[x] = v.x;
+        xi[x] = v.y;
+    }
+    __syncwarp();
+    double *orr, *oi;
+    FFTRun<double, N, 0, 1>::run(xr, xi, yr, yi, twr, twi, lane, inverse != 0, 1.0, 1.0, orr, oi);
+    __syncwarp();
+    for (int x = lane; x < N; x += WARP) d[x] = make_double2(orr[x], oi[x]);
+}
+
+// t transform of complex columns in place: column (b, x) of length nt, stride nx.
+// wt[m] = exp(-2 pi i m / nt); inverse uses the conjugate.
+__global__ void __launch_bounds__(TT_THREADS) tt_dft_t_kernel(double2 *data, int nt, int nx, const double2 *wt,
+                                                              int inverse)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double2 *tile = reinterpret_cast<double2 *>(smem_raw);  // [nt][TT_COLS]
+    double2 *w = tile + (size_t)nt * TT_COLS;                // [nt]
+    const int x0 = blockIdx.x * TT_COLS;
+    double2 *base = data + (size_t)blockIdx.y * nt * nx + x0;
+    for (int idx = threadIdx.x; idx < nt * TT_COLS; idx += TT_THREADS) {
+        const int t = idx / TT_COLS, c = idx % TT_COLS;
+        tile[idx] = (x0 + c < nx) ? base[(size_t)t * nx + c] : make_double2(0.0, 0.0);
+    }
+    for (int m = threadIdx.x; m < nt; m += TT_THREADS) {
+        double2 v = wt[m];
+        if (inverse) v.y = -v.y;
+        w[m] = v;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nt * TT_COLS; idx += TT_THREADS) {
+        const int k = idx / TT_COLS, c = idx % TT_COLS;
+        double sr = 0.0, si = 0.0;
+        int m = 0;
+        for (int t = 0; t < nt; t++) {
+            const double2 a = tile[t * TT_COLS + c], b = w[m];
+            sr += a.x * b.x - a.y * b.y;
+            si += a.x * b.y + a.y * b.x;
+            m += k;
+            if (m >= nt) m -= nt;
+        }
+        if (x0 + c < nx) base[(size_t)k * nx + c] = make_double2(sr, si);
+    }
+}
+
+// out = in * filter[t][x] (real), optionally times i 2 pi freqnu(t) (the time derivative of
+// driver.f90:2015-2017, freqnu = distmat(nt) / (nt dt 60)).
+__global__ void __launch_bounds__(TT_THREADS) tt_filter_kernel(const double2 *in, double2 *out, const double *filter,
+                                                               int nt, int nx, long long n, int deriv, double dt_min)
+{
+    const long long stride = (long long)gridDim.x * TT_THREADS;
+    for (long long i = (long long)blockIdx.x * TT_THREADS + threadIdx.x; i < n; i += stride) {
+        const long long tx = i % ((long long)nt * nx);
+        const int t = (int)(tx / nx);
+        const double f = filter[tx];
+        double2 v = in[i];
+        v.x *= f;
+        v.y *= f;
+        if (deriv) {
+            const int d = (t > nt - t) ? -(nt - t) : t;  // distmat: index 0 at 0, upper half negative
+            const double om = 2.0 * TT_PI * ((double)d / ((double)nt * dt_min * 60.0));
+            v = make_double2(-om * v.y, om * v.x);  // times i om
+        }
+        out[i] = v;
+    }
+}
+
+// Real records into complex planes.
+__global__ void __launch_bounds__(TT_THREADS) tt_load_kernel(const double *in, double2 *out, long long n)
+{
+    const long long stride = (long long)gridDim.x * TT_THREADS;
+    for (long long i = (long long)blockIdx.x * TT_THREADS + threadIdx.x; i < n; i += stride)
+        out[i] = make_double2(in[i], 0.0);
+}
+
+// Real part into a complex buffer (imaginary part zero), optional scale.
+__global__ void __launch_bounds__(TT_THREADS) tt_real_kernel(const double2 *in, double2 *out, long long n, double s)
+{
+    const long long stride = (long long)gridDim.x * TT_THREADS;
+    for (long long i = (long long)blockIdx.x * TT_THREADS + threadIdx.x; i < n; i += stride)
+        out[i] = make_double2(in[i].x * s, 0.0);
+}
+
+// Multiplier of COMPUTE_TT_GIZONBIRCH's derivative (driver.f90:913-917) on the full spectrum:
+// i 2 pi q / (nt dt) below nt/2, zero at q = nt/2 (and its mirror), the conjugate mirror above.
+__global__ void __launch_bounds__(TT_THREADS) tt_gb_kernel(double2 *data, int nt, int nx, long long n, double dt_min)
+{
+    const int h = nt / 2;
+    const long long stride = (long long)gridDim.x * TT_THREADS;
+    for (long long i = (long long)blockIdx.x * TT_THREADS + threadIdx.x; i < n; i += stride) {
+        const int q = (int)((i / nx) % nt);
+        int s = 0;
+        if (q < h) s = q;
+        else if (q > nt - h) s = -(nt - q);
+        const double om = 2.0 * TT_PI * (double)s / ((double)nt * dt_min);
+        const double2 v = data[i];
+        data[i] = make_double2(-om * v.y, om * v.x);
+    }
+}
+
+// One measured receiver: b, x (0-based), search range [timest, timefin] (1-based, clipped),
+// given window (lef, rig) or picked one; results: lef, rig, loc, tau, con.
+struct TTRow {
+    int b, x, timest, timefin, lef, rig, loc, pad;
+    double tau, con;
+};
+
+// One warp per measured receiver (driver.f90:2040-2100): window pick (first maximum of
+// |Re acc| over the search range), travel time by Simpson sums (SIMPSON_REGULAR weights over
+// the whole record, integrals.f90:107-130) of w u0dot (u0 - u) and w u0dot^2, and the
+// normalisation con = Re(-tau / (sum_{lef..rig} ccdot^2 dt)).  u0dot holds nt times the
+// derivative (the c2r transform is unnormalised).
+__global__ void __launch_bounds__(TT_THREADS) tt_rows_kernel(TTRow *rows, int nrows, const double2 *acc,
+                                                             const double2 *dat, const double2 *u0dot,
+                                                             const double2 *ccdot, int nt, int nx, int halftime,
+                                                             int given, double dt_min)
+{
+    const int warp = (blockIdx.x * TT_THREADS + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nrows) return;
+    TTRow r = rows[warp];
+    const size_t base = (size_t)r.b * nt * nx + r.x;
+    auto at = [&](const double2 *f, int t) { return f[base + (size_t)t * nx]; };
+    if (!given) {
+        const int a = max(r.timest, 1), e = min(r.timefin, nt);
+        double best = -1.0;
+        int bi = a;
+        for (int t = a + lane; t <= e; t += WARP) {
+            const double v = fabs(at(acc, t - 1).x);
+            if (v > best) { best = v; bi = t; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        r.loc = bi;
+        r.lef = max(bi - halftime, 1);
+        r.rig = min(bi + halftime, nt);
+    }
+    double num = 0.0, den = 0.0, sr = 0.0, si = 0.0;
+    const double inv_nt = 1.0 / (double)nt;
+    for (int t = r.lef + lane; t <= r.rig; t += WARP) {  // 1-based t
+        const double wgt = (t == 1 || t == nt) ? 1.0 : ((t % 2 == 0) ? 4.0 : 2.0);
+        const double ud = at(u0dot, t - 1).x * inv_nt;
+        const double u0 = at(acc, t - 1).x, u = at(dat, t - 1).x;
+        num += wgt * (ud * (u0 - u));
+        den += wgt * (ud * ud);
+        const double2 c = at(ccdot, t - 1);
+        sr += c.x * c.x - c.y * c.y;
+        si += 2.0 * c.x * c.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        num += __shfl_xor_sync(0xffffffffu, num, o);
+        den += __shfl_xor_sync(0xffffffffu, den, o);
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (lane == 0) {
+        const double tau = num / den;  // both Simpson sums carry the same dt / 3
+        const double dr = sr * dt_min, di = si * dt_min;
+        r.tau = tau;
+        r.con = -tau * dr / (dr * dr + di * di);  // Re(-tau / (dr + i di))
+        rows[warp] = r;
+    }
+}
+
+// c(x_i, t) = con_i w_i(t) ccdot(x_i, t) at the measured receivers (the buffer is zeroed first).
+__global__ void __launch_bounds__(TT_THREADS) tt_scatter_kernel(const TTRow *rows, int nrows, const double2 *ccdot,
+                                                                double2 *c, int nt, int nx)
+{
+    const int warp = (blockIdx.x * TT_THREADS + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nrows) return;
+    const TTRow r = rows[warp];
+    const size_t base = (size_t)r.b * nt * nx + r.x;
+    for (int t = r.lef + lane; t <= r.rig; t += WARP) {
+        const double2 v = ccdot[base + (size_t)(t - 1) * nx];
+        double2 &o = c[base + (size_t)(t - 1) * nx];
+        o.x += r.con * v.x;
+        o.y += r.con * v.y;
+    }
+}
+
+// adj[b][nt-1-t][x] += Re(field[b][t][x]) (time reversal, driver.f90:2097-2099).
+__global__ void __launch_bounds__(TT_THREADS) tt_accum_kernel(const double2 *f, double *adj, int nt, int nx,
+                                                              long long n)
+{
+    const long long stride = (long long)gridDim.x * TT_THREADS;
+    for (long long i = (long long)blockIdx.x * TT_THREADS + threadIdx.x; i < n; i += stride) {
+        const long long plane = (long long)nt * nx;
+        const long long b = i / plane, r = i - b * plane;
+        const int t = (int)(r / nx), x = (int)(r - (long long)t * nx);
+        adj[b * plane + (long long)(nt - 1 - t) * nx + x] += f[i].x;
+    }
+}
+
+__global__ void __launch_bounds__(TT_THREADS) tt_scale_out_kernel(const double *adj, double *out, long long n, double s)
+{
+    const long long stride = (long long)gridDim.x * TT_THREADS;
+    for (long long i = (long long)blockIdx.x * TT_THREADS + threadIdx.x; i < n; i += stride) out[i] = adj[i] * s;
+}
+
+unsigned tt_grid(long long n)
+{
+    const long long g = (n + TT_THREADS - 1) / TT_THREADS;
+    return (unsigned)(g < 152LL * 8 ? g : 152LL * 8);
+}
+
+}  // namespace
+
+struct sparc_tt_plan {
+    int nx = 0, nt = 0, nb = 0;
+    std::vector<void *> allocs;
+    double2 *S = nullptr, *D = nullptr, *ACC = nullptr, *DAT = nullptr, *CCD = nullptr, *U0D = nullptr, *C = nullptr;
+    double *adj = nullptr, *twr = nullptr, *twi = nullptr;
+    double2 *wt = nullptr;
+    TTRow *rows = nullptr;
+    int cap = 0;
+};
+
+namespace {
+
+template <int N>
+cudaError_t fft_x_n(sparc_tt_plan *p, double2 *f, int inverse, cudaStream_t st)
+{
+    const long long nrows = (long long)p->nb * p->nt;
+    const size_t smem = (size_t)TT_XWPB * 4 * N * sizeof(double);
+    auto k = tt_fft_x_kernel<N>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<(unsigned)((nrows + TT_XWPB - 1) / TT_XWPB), TT_XWPB * WARP, smem, st>>>(f, nrows, p->twr, p->twi, inverse);
+    return cudaGetLastError();
+}
+
+cudaError_t fft_x(sparc_tt_plan *p, double2 *f, int inverse, cudaStream_t st)
+{
+#define CASE(n_) if (p->nx == n_) return fft_x_n<n_>(p, f, inverse, st);
+    CASE(64) CASE(128) CASE(192) CASE(256) CASE(384) CASE(512) CASE(768) CASE(1024)
+#undef CASE
+    return cudaErrorInvalidValue;
+}
+
+size_t dft_t_smem(int nt) { return ((size_t)nt * TT_COLS + nt) * sizeof(double2); }
+
+cudaError_t dft_t(sparc_tt_plan *p, double2 *f, int inverse, cudaStream_t st)
+{
+    const size_t smem = dft_t_smem(p->nt);
+    cudaError_t e = cudaFuncSetAttribute(tt_dft_t_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((p->nx + TT_COLS - 1) / TT_COLS, p->nb);
+    tt_dft_t_kernel<<<grid, TT_THREADS, smem, st>>>(f, p->nt, p->nx, p->wt, inverse);
+    return cudaGetLastError();
+}
+
+// 2-D transform over (x, t) of every source's plane.
+cudaError_t dft2(sparc_tt_plan *p, double2 *f, int inverse, cudaStream_t st)
+{
+    cudaError_t e = fft_x(p, f, inverse, st);
+    if (e == cudaSuccess) e = dft_t(p, f, inverse, st);
+    return e;
+}
+
+int tt_fail(const char *what, cudaError_t e)
+{
+    return report_error(SPARC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool tt_nx_ok(int nx)
+{
+    return nx == 64 || nx == 128 || nx == 192 || nx == 256 || nx == 384 || nx == 512 || nx == 768 || nx == 1024;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sparc_tt_plan_create(int nx, int nt, int nbatch, int max_rows, sparc_tt_plan_t **out)
+{
+    if (!out) return report_error(SPARC_ERR_ARG, "sparc_tt_plan_create: null argument");
+    *out = nullptr;
+    if (!tt_nx_ok(nx)) return report_error(SPARC_ERR_SIZE, "sparc_tt_plan_create: nx not in the FFT table");
+    if (nt < 2 || dft_t_smem(nt) > 220 * 1024)
+        return report_error(SPARC_ERR_SIZE, "sparc_tt_plan_create: nt must be in 2..860");
+    if (nbatch < 1 || nbatch > 65535 || max_rows < 1) return report_error(SPARC_ERR_ARG, "sparc_tt_plan_create: bad batch");
+    sparc_tt_plan *p = new sparc_tt_plan();
+    p->nx = nx;
+    p->nt = nt;
+    p->nb = nbatch;
+    p->cap = max_rows;
+    const size_t n = (size_t)nbatch * nt * nx;
+    struct Req { void **ptr; size_t bytes; };
+    std::vector<Req> reqs = {
+        {(void **)&p->S, n * sizeof(double2)}, {(void **)&p->D, n * sizeof(double2)},
+        {(void **)&p->ACC, n * sizeof(double2)}, {(void **)&p->DAT, n * sizeof(double2)},
+        {(void **)&p->CCD, n * sizeof(double2)}, {(void **)&p->U0D, n * sizeof(double2)},
+        {(void **)&p->C, n * sizeof(double2)}, {(void **)&p->adj, n * sizeof(double)},
+        {(void **)&p->twr, nx * sizeof(double)}, {(void **)&p->twi, nx * sizeof(double)},
+        {(void **)&p->wt, nt * sizeof(double2)}, {(void **)&p->rows, (size_t)max_rows * sizeof(TTRow)},
+    };
+    for (auto &r : reqs) {
+        cudaError_t e = cudaMalloc(r.ptr, r.bytes);
+        if (e != cudaSuccess) {
+            sparc_tt_plan_destroy(p);
+            return tt_fail("sparc_tt_plan_create: cudaMalloc", e);
+        }
+        p->allocs.push_back(*r.ptr);
+    }
+    std::vector<double> tr(nx), ti(nx);
+    for (int t = 0; t < nx; t++) {
+        tr[t] = std::cos(2.0 * TT_PI * (double)t / (double)nx);
+        ti[t] = -std::sin(2.0 * TT_PI * (double)t / (double)nx);
+    }
+    std::vector<double2> w(nt);
+    for (int m = 0; m < nt; m++) w[m] = make_double2(std::cos(2.0 * TT_PI * (double)m / (double)nt),
+                                                     -std::sin(2.0 * TT_PI * (double)m / (double)nt));
+    cudaError_t e = cudaMemcpy(p->twr, tr.data(), nx * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->twi, ti.data(), nx * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(p->wt, w.data(), nt * sizeof(double2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(p->adj, 0, n * sizeof(double));
+    if (e != cudaSuccess) {
+        sparc_tt_plan_destroy(p);
+        return tt_fail("sparc_tt_plan_create: tables", e);
+    }
+    *out = p;
+    return SPARC_OK;
+}
+
+int sparc_tt_plan_destroy(sparc_tt_plan_t *p)
+{
+    if (!p) return SPARC_OK;
+    for (void *q : p->allocs) cudaFree(q);
+    delete p;
+    return SPARC_OK;
+}
+
+int sparc_tt_set_records(sparc_tt_plan_t *p, const double *synth, const double *data, void *stream)
+{
+    if (!p || !synth || !data) return report_error(SPARC_ERR_ARG, "sparc_tt_set_records: null argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const long long n = (long long)p->nb * p->nt * p->nx;
+    // real records into complex planes, then forward 2-D transforms (driver.f90:1840-1844)
+    tt_load_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(synth, p->S, n);
+    tt_load_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(data, p->D, n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = dft2(p, p->S, 0, st);
+    if (e == cudaSuccess) e = dft2(p, p->D, 0, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p->adj, 0, (size_t)n * sizeof(double), st);
+    return e == cudaSuccess ? SPARC_OK : tt_fail("sparc_tt_set_records", e);
+}
+
+int sparc_tt_mode(sparc_tt_plan_t *p, const double *filter, int nrows, int *rows, int halftime, int given,
+                  double dt_min, double *tau, void *stream)
+{
+    if (!p || !filter || nrows < 0 || nrows > p->cap || (nrows > 0 && (!rows || !tau)) || halftime < 0)
+        return report_error(SPARC_ERR_ARG, "sparc_tt_mode: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nt = p->nt, nx = p->nx;
+    const long long n = (long long)p->nb * nt * nx;
+    for (int r = 0; r < nrows; r++) {
+        const int *q = rows + 7 * r;
+        if (q[0] < 0 || q[0] >= p->nb || q[1] < 0 || q[1] >= nx || (given && (q[4] < 1 || q[5] > nt || q[4] > q[5])))
+            return report_error(SPARC_ERR_ARG, "sparc_tt_mode: row out of range");
+        if (!given && (max(q[2], 1) > min(q[3], nt)))
+            return report_error(SPARC_ERR_ARG, "sparc_tt_mode: empty search range");
+    }
+    std::vector<TTRow> h(nrows);
+    for (int r = 0; r < nrows; r++) {
+        const int *q = rows + 7 * r;
+        h[r] = TTRow{q[0], q[1], q[2], q[3], q[4], q[5], 0, 0, 0.0, 0.0};
+    }
+    cudaError_t e = cudaSuccess;
+    // filtered synthetic and data, the time derivative of the filtered synthetic (driver.f90:1990-2017)
+    tt_filter_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->S, p->ACC, filter, nt, nx, n, 0, dt_min);
+    tt_filter_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->D, p->DAT, filter, nt, nx, n, 0, dt_min);
+    tt_filter_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->S, p->CCD, filter, nt, nx, n, 1, dt_min);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = dft2(p, p->ACC, 1, st);
+    if (e == cudaSuccess) e = dft2(p, p->DAT, 1, st);
+    if (e == cudaSuccess) e = dft2(p, p->CCD, 1, st);
+    // Gizon-Birch derivative of every synthetic column along t (driver.f90:905-923)
+    if (e == cudaSuccess) {
+        tt_real_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->ACC, p->U0D, n, 1.0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = dft_t(p, p->U0D, 0, st);
+    if (e == cudaSuccess) {
+        tt_gb_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->U0D, nt, nx, n, dt_min);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = dft_t(p, p->U0D, 1, st);
+    if (e == cudaSuccess && nrows > 0) {
+        e = cudaMemcpyAsync(p->rows, h.data(), nrows * sizeof(TTRow), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            const unsigned g = (unsigned)(((long long)nrows * WARP + TT_THREADS - 1) / TT_THREADS);
+            tt_rows_kernel<<<g, TT_THREADS, 0, st>>>(p->rows, nrows, p->ACC, p->DAT, p->U0D, p->CCD, nt, nx, halftime,
+                                                     given, dt_min);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemsetAsync(p->C, 0, (size_t)n * sizeof(double2), st);
+        if (e == cudaSuccess) {
+            const unsigned g = (unsigned)(((long long)nrows * WARP + TT_THREADS - 1) / TT_THREADS);
+            tt_scatter_kernel<<<g, TT_THREADS, 0, st>>>(p->rows, nrows, p->CCD, p->C, nt, nx);
+            e = cudaGetLastError();
+        }
+        // adj_mode = Re IDFT2(filter * DFT2(c)), accumulated time-reversed
+        if (e == cudaSuccess) e = dft2(p, p->C, 0, st);
+        if (e == cudaSuccess) {
+            tt_filter_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->C, p->C, filter, nt, nx, n, 0, dt_min);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = dft2(p, p->C, 1, st);
+        if (e == cudaSuccess) {
+            tt_accum_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->C, p->adj, nt, nx, n);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), p->rows, nrows * sizeof(TTRow), cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return tt_fail("sparc_tt_mode", e);
+    for (int r = 0; r < nrows; r++) {
+        int *q = rows + 7 * r;
+        q[4] = h[r].lef;
+        q[5] = h[r].rig;
+        q[6] = h[r].loc;
+        tau[r] = h[r].tau;
+    }
+    return SPARC_OK;
+}
+
+int sparc_tt_adjoint(sparc_tt_plan_t *p, double *adj, void *stream)
+{
+    if (!p || !adj) return report_error(SPARC_ERR_ARG, "sparc_tt_adjoint: null argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const long long n = (long long)p->nb * p->nt * p->nx;
+    tt_scale_out_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->adj, adj, n, (double)p->nt / 60.0);  // driver.f90:2201
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? SPARC_OK : tt_fail("sparc_tt_adjoint", e);
+}
+
+}  // extern "C"

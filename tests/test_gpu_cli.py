@@ -59,7 +59,8 @@ def test_forward_adjoint_kernel_files(tmp_path):
     run = RunConfig(nx=128, nz=300, xlength_cm=200e8, nsteps=46)
     psi = M.gaussian_psi(run, M.polytrope(300), 0.05)
     fits.write(str(data / "model_psi_ls00.fits"), psi[:, None, :])
-    env = dict(os.environ, SPARC_NSTEPS="46", SPARC_PRECISION="64")
+    # the waveform adjoint source: no params.<pord> files, so the travel-time source would be zero
+    env = dict(os.environ, SPARC_NSTEPS="46", SPARC_PRECISION="64", SPARC_ADJOINT_SOURCE="waveform")
     shutil.copy(os.path.join(ROOT, "tests", "golden", "Spectral"), code / "Instruction_src02_ls00")
     r = run_sparc(code, "02", "00", env)
     assert r.returncode == 0, r.stderr
@@ -79,6 +80,42 @@ def test_forward_adjoint_kernel_files(tmp_path):
         assert k.shape == (300, 1, 128) and np.all(np.isfinite(k)), name
     assert np.abs(fits.read(str(data / "kernel" / "kernel_c_02.fits"))).max() > 0
     assert not (fdir / "partial_states.npy").exists()
+
+
+def test_forward_writes_the_travel_time_adjoint_source(tmp_path):
+    """A forward run with params.0 present measures f-mode travel times (ADJOINT_SOURCE_FILT):
+    ttdiff.0, windows.0, adjoint_src02/{source.fits, information}, kernel/misfit_02_00."""
+    code = tmp_path / "code"
+    data = tmp_path / "data_dir"
+    code.mkdir()
+    (data / "data").mkdir(parents=True)
+    (code / "params.i").write_text(PARAMS.format(dir=str(data)))
+    np.savetxt(code / "polytrope_gen", M.polytrope(300), fmt="%.17e")
+    (data / "master.pixels").write_text("-10.0\n15.0\n")
+    (data / "params.0").write_text("3.0\n9.0\n6.0\n")
+    nsteps = 601
+    env = dict(os.environ, SPARC_NSTEPS=str(nsteps), SPARC_PRECISION="64")
+    # observed data: the synthetic of a run with the source 0.4 Mm further away
+    (data / "master.pixels").write_text("-10.0\n15.4\n")
+    open(code / "compute_data", "w").close()
+    shutil.copy(os.path.join(ROOT, "tests", "golden", "Spectral"), code / "Instruction_src02_ls00")
+    assert run_sparc(code, "02", "00", env).returncode == 0
+    os.remove(code / "compute_data")
+    shutil.copy(data / "forward_src02_ls00" / "vz_cc.fits", data / "data" / "02.fits")
+    (data / "master.pixels").write_text("-10.0\n15.0\n")
+    shutil.copy(os.path.join(ROOT, "tests", "golden", "Spectral"), code / "Instruction_src02_ls00")
+    r = run_sparc(code, "02", "00", env)
+    assert r.returncode == 0, r.stderr
+    rows = np.loadtxt(data / "forward_src02_ls00" / "ttdiff.0", ndmin=2)
+    assert rows.shape[1] == 7 and rows.shape[0] > 0 and np.isfinite(rows[:, 1]).all()
+    win = np.loadtxt(data / "forward_src02_ls00" / "windows.0", ndmin=2)
+    assert win.shape == (rows.shape[0], 2)
+    src = fits.read(str(data / "adjoint_src02" / "source.fits"))
+    assert src.shape == (nsteps // 15 + 1, 1, 128) and np.isfinite(src).all() and np.abs(src).max() > 0
+    info = (data / "adjoint_src02" / "information").read_text().split()
+    assert int(info[0]) == nsteps // 15 + 1 and info[-1] == "2D"
+    mis = np.loadtxt(data / "kernel" / "misfit_02_00")
+    assert int(mis[0]) == 2 and int(mis[1]) == rows.shape[0] and mis[2] > 0
 
 
 def test_unknown_source_fails_with_nonzero_status(tmp_path):
