@@ -236,6 +236,50 @@ def gradient_stage(pipe, model, dev, reps=20, cpu=True):
     return out
 
 
+def tt_stage(seis, run, specs, dev, cpu=True):
+    """The travel-time adjoint source (ADJOINT_SOURCE_FILT) of every source of the batch from its
+    own seismograms: all nine ridge filters with 5-60 Mm receiver ranges and 10-20 min windows,
+    data = the synthetic one record later plus noise.  GPU time with CUDA events around
+    TTAdjoint.run; the oracle's per-receiver restatement timed on one host core for one source."""
+    import numpy as np
+    import torch
+
+    from sparc_flows_gb300.ttadjoint import TTAdjoint
+
+    s = seis.double().contiguous()
+    nb, nt, nx = s.shape
+    g = torch.Generator(device="cpu").manual_seed(0)
+    d = (torch.roll(s, 1, dims=1) + 0.05 * s.abs().max() * torch.randn(s.shape, generator=g, dtype=torch.float64).to(dev)).contiguous()
+    modes = {p: (5.0, 60.0, 10.0 + p) for p in range(9)}
+    freq = {"allmodes": (1.5, 6.0)}
+    t_min = np.arange(nt) * (run.outputcad / 60.0)
+    x00s = [sp.xloc for sp in specs]
+    tt = TTAdjoint(nx, nt, nb, run.xlength_cm, run.outputcad, device=dev)
+    tt.run(s, d, x00s, t_min, modes, freq)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    res = tt.run(s, d, x00s, t_min, modes, freq)
+    e1.record()
+    torch.cuda.synchronize()
+    gpu_ms = e0.elapsed_time(e1)
+    out = {"workload": f"{nb} sources, {nt} records x {nx} columns, 9 ridge filters, FP64 (driver.f90:1758-2238)",
+           "gpu_ms_all_sources": gpu_ms, "measurements": int(res["nmeas"].sum())}
+    if cpu:
+        from oracle import tt_oracle as TO
+        t0 = time.perf_counter()
+        ref = TO.adjoint_source(s[0].cpu().numpy(), d[0].cpu().numpy(), x00s[0], run.xlength_cm, t_min,
+                                run.outputcad, modes, freq)
+        cpu_s = time.perf_counter() - t0
+        a = res["adj"][0].cpu().numpy()
+        out["cpu_numpy_ms_one_source"] = cpu_s * 1e3
+        out["cpu_kind"] = "port (per-receiver 2-D transforms as the reference, numpy.fft, 1 core)"
+        out["gpu_ms_per_source"] = gpu_ms / nb
+        out["rel_err_vs_oracle_source0"] = float(np.linalg.norm(a - ref["adj"]) / max(np.linalg.norm(ref["adj"]), 1e-300))
+    tt.close()
+    return out
+
+
 # ----------------------------------------------------------------------------------------------
 def run_gpu(args):
     import numpy as np
@@ -382,6 +426,7 @@ def run_gpu(args):
             line["accuracy"] = accuracy
         if not args.no_gradient:
             line["gradient"] = gradient_stage(pipe, model, dev, cpu=not args.no_cpu)
+            line["tt_adjoint_source"] = tt_stage(seis_h.to(dev), run, specs, dev, cpu=not args.no_cpu)
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_quick()
         print(json.dumps(line), flush=True)

@@ -40,9 +40,6 @@ _RIDGE = {
 }
 _P2_CONST = 4.1004  # driver.f90:1320
 MODE_SPEED = [0.44, 0.60, 0.75, 0.9, 1.2, 1.4, 1.7, 1.9]  # vel(0:7), driver.f90:1936-1944
-FILTER_FITS = ["fmode_filter.fits", "p1mode_filter.fits", "p2mode_filter.fits", "p3mode_filter.fits",
-               "p4mode_filter.fits", "p5mode_filter.fits", "p6mode_filter.fits", "p7mode_filter.fits",
-               "first_bounce_pmode_filter.fits"]
 
 
 def signed_index(n: int) -> np.ndarray:
@@ -266,13 +263,13 @@ def write_outputs(directory: str, contrib: str, jobno: str, res: dict, b: int, t
     if not linesearch:
         os.makedirs(adir, exist_ok=True)
         with open(os.path.join(adir, "information"), "w") as fh:
-            fh.write(f"{len(t_min)}\n{t_min[0] * 60.0!r}\n{t_min[-1] * 60.0!r}\n")
+            fh.write(f"{len(t_min)}\n{float(t_min[0]) * 60.0!r}\n{float(t_min[-1]) * 60.0!r}\n")
             if test_in_2d:
                 fh.write("2D\n")
     kdir = os.path.join(directory, "kernel")
     os.makedirs(kdir, exist_ok=True)
     with open(os.path.join(kdir, f"misfit_{contrib}_{jobno}"), "w") as fh:
-        fh.write(f"{int(contrib):12d}{int(res['nmeas'][b]):12d}  {res['misfit'][b]!r}\n")
+        fh.write(f"{int(contrib):12d}{int(res['nmeas'][b]):12d}  {float(res['misfit'][b])!r}\n")
 
 
 def read_windows(directory: str, contrib: str, modes: dict) -> dict:
