@@ -277,6 +277,14 @@ int sparc_tt_set_records(sparc_tt_plan_t *plan, const double *synth, const doubl
 int sparc_tt_mode(sparc_tt_plan_t *plan, const double *filter, int nrows, int *rows, int halftime, int given,
                   double dt_min, double *tau, void *stream);
 
+/* MISFIT_ALL (driver.f90:2294-2651) for one ridge filter of one frequency band: filter as in
+ * sparc_tt_mode; rows as in sparc_tt_mode with the window loc -+ halftime not clipped; tau: host
+ * [nrows] out, COMPUTE_TT (driver.f90:855-890) cross-correlation travel times in minutes, NaN
+ * where the window leaves the record or the correlation peak sits at the end of its lag range
+ * (the reference reads past its arrays there).  Does not touch the adjoint source. */
+int sparc_tt_misfit_mode(sparc_tt_plan_t *plan, const double *filter, int nrows, int *rows, int halftime,
+                         int given, double dt_min, double *tau, void *stream);
+
 /* The adjoint source of every source, [nbatch][nt][nx] device, times nt / 60 (driver.f90:2201),
  * in the reference's time-reversed order (ready for source.fits). */
 int sparc_tt_adjoint(sparc_tt_plan_t *plan, double *adj, void *stream);

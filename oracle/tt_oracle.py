@@ -235,3 +235,99 @@ def adjoint_source(synth: np.ndarray, data: np.ndarray, x00: float, xlength_cm: 
         rows_out[pord], win_out[pord] = rows, wins
     adj = adj * nt / 60.0
     return {"adj": adj, "misfit": misfit, "nmeas": nmeas, "rows": rows_out, "windows": win_out}
+
+
+# ---------------------------------------------------------------------------------------------
+# MISFIT_ALL (driver.f90:2294-2651): travel times by cross-correlation in three frequency bands
+# ---------------------------------------------------------------------------------------------
+BANDS = [(2.0, 3.5), (3.5, 4.5), (4.5, 6.0)]  # driver.f90:2376-2385
+
+
+def compute_tt(u0: np.ndarray, u: np.ndarray, dt: float):
+    """COMPUTE_TT (driver.f90:855-890): peak of the cross-correlation refined by the parabola
+    through its three samples (the 3 x 3 system solved by inversion).  None when the peak sits
+    at the end of the lag range (the reference reads past the array there)."""
+    n = len(u0)
+    lags = np.arange(-n + 1, n)
+    cc = np.zeros(2 * n - 1)
+    for j, i in enumerate(lags):
+        if i <= 0:
+            l1 = -i + 1
+            cc[j] = np.sum(u0[l1 - 1:n] * u[0:n - l1 + 1]) * dt
+        else:
+            l2 = n - i
+            cc[j] = np.sum(u0[0:l2] * u[i:n]) * dt
+    jm = int(np.argmax(cc))
+    if jm == 0 or jm == 2 * n - 2:
+        return None
+    loc = lags[jm]
+    times = np.array([(loc - 1) * dt, loc * dt, (loc + 1) * dt])
+    mat = np.stack([np.ones(3), times, times ** 2], axis=1)
+    inv = np.linalg.inv(mat)
+    c3 = cc[jm - 1:jm + 2]
+    p1 = inv[1] @ c3
+    p2 = inv[2] @ c3
+    return -p1 * 0.5 / p2
+
+
+def misfit_search_range(pord: int, dist: float, dt: float):
+    """timest, timefin of MISFIT_ALL's window pick (driver.f90:2436-2446): the f/p modes as in
+    ADJOINT_SOURCE_FILT, the first bounce with its own polynomials."""
+    if pord != 8:
+        ts = math.floor(dist / F32(VEL[pord]) * (1.0 / dt))
+        return ts, ts + 40
+    ts = math.floor((F32(-1.45511095e-04) * dist ** 2 + F32(2.72140632e-01) * dist + F32(2.16331969e+01)) * (1.0 / dt))
+    tf = math.floor((F32(3.85746516e-08) * dist ** 2 + F32(2.21324786e-01) * dist + F32(4.36702155e+01)) * (1.0 / dt))
+    return ts, tf
+
+
+def misfit_all(synth: np.ndarray, data: np.ndarray, x00: float, xlength_cm: float, t_min: np.ndarray,
+               outputcad: float, modes: dict, windows: dict | None = None):
+    """MISFIT_ALL for one source.  Returns a list over the three bands of dict(band, nmeas (11,),
+    misfit (11,) halved, windows {pord: [(lef, rig)]}) -- windows as picked, unclipped; a window
+    that leaves the record, or a correlation peak at the end of its lag range, is not measured."""
+    nt, nx = synth.shape
+    dt = t_min[1] - t_min[0]
+    x = np.arange(nx) / nx
+    distances = np.abs((x - 0.5) * xlength_cm * F32(1e-8) - x00)
+    tempout = np.fft.fft2(synth)
+    tempdat = np.fft.fft2(data)
+    out = []
+    for fb, (left, right) in enumerate(BANDS, start=1):
+        filt = freq_filter(left, right, nt, outputcad)
+        nmeas = np.zeros(11, dtype=int)
+        mis = np.zeros(11)
+        wins = {}
+        for pord in range(9):
+            if pord not in modes:
+                continue
+            mindist, maxdist, window = modes[pord]
+            halftime = int(math.floor(window / (2.0 * dt) + 0.5))
+            filt2 = ridge_filter(pord, nx, nt, xlength_cm, outputcad) * filt[:, None]
+            acc = (np.fft.ifft2(tempout * filt2) * (nx * nt)).real
+            dat = (np.fft.ifft2(tempdat * filt2) * (nx * nt)).real
+            given = iter(windows[fb][pord]) if windows and fb in windows and pord in windows[fb] else None
+            wl = []
+            for i in range(nx):
+                if not (distances[i] > mindist and distances[i] < maxdist):
+                    continue
+                if given is None:
+                    ts, tf = misfit_search_range(pord, distances[i], dt)
+                    a, b = max(ts, 1), min(tf, nt)
+                    if a > b:
+                        continue
+                    loc = int(np.argmax(np.abs(acc[a - 1:b, i]))) + a
+                    lef, rig = loc - halftime, loc + halftime
+                else:
+                    lef, rig = next(given)
+                wl.append((lef, rig))
+                if lef < 1 or rig > nt:
+                    continue
+                tau = compute_tt(acc[lef - 1:rig, i], dat[lef - 1:rig, i], dt)
+                if tau is None:
+                    continue
+                mis[pord] += tau ** 2
+                nmeas[pord] += 1
+            wins[pord] = wl
+        out.append({"band": (left, right), "nmeas": nmeas, "misfit": 0.5 * mis, "windows": wins})
+    return out

@@ -56,6 +56,8 @@ SIGNATURES = {
     "sparc_tt_set_records": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "sparc_tt_mode": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp,
                                      _vp]),
+    "sparc_tt_misfit_mode": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_double, _dp, _vp]),
     "sparc_tt_adjoint": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_grad_workspace_bytes": (ctypes.c_ulonglong, [ctypes.c_int, ctypes.c_int]),
     "sparc_gradient": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),

@@ -149,11 +149,13 @@ def _forward(run, model, directory, contrib, jobno, src, precision, device, comp
 
 
 def _tt_adjoint(run, directory, contrib, jobno, xloc, synth, data, device):
-    """ADJOINT_SOURCE_FILT (driver.f90:1758-2238) after a forward run that is not a data run:
-    travel times of the ridge-filtered records, adjoint source, misfit files."""
+    """ADJOINT_SOURCE_FILT (driver.f90:1758-2238) and MISFIT_ALL (driver.f90:2294-2651) after a
+    forward run that is not a data run: travel times of the ridge-filtered records, adjoint
+    source, misfit files."""
     import torch
 
-    from .ttadjoint import TTAdjoint, read_measurement_files, read_windows, write_outputs
+    from .ttadjoint import (TTAdjoint, read_measurement_files, read_windows, read_windows_all, write_misfit_all,
+                            write_outputs)
 
     linesearch = os.path.exists("linesearch")
     tl = np.loadtxt(os.path.join(directory, f"forward_src{contrib}_ls{jobno}", "timeline"), ndmin=2)[:, 1]
@@ -163,6 +165,10 @@ def _tt_adjoint(run, directory, contrib, jobno, xloc, synth, data, device):
     tt = TTAdjoint(run.nx, synth.shape[0], 1, run.xlength_cm, float(run.outputcad), device=device)
     res = tt.run(torch.as_tensor(synth[None]), torch.as_tensor(data[None]), [xloc], t_min, modes, freq, windows)
     write_outputs(directory, contrib, jobno, res, 0, t_min, linesearch, os.path.exists("compute_synth"))
+    # MISFIT_ALL (driver.f90:276, 2294-2651)
+    wall = read_windows_all(directory, contrib, modes) if linesearch else None
+    bands = tt.misfit_all(torch.as_tensor(synth[None]), torch.as_tensor(data[None]), [xloc], t_min, modes, wall)
+    write_misfit_all(directory, contrib, jobno, bands, 0, linesearch)
     tt.close()
 
 

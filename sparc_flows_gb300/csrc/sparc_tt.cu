@@ -218,6 +218,80 @@ __global__ void __launch_bounds__(TT_THREADS) tt_rows_kernel(TTRow *rows, int nr
     }
 }
 
+// MISFIT_ALL (driver.f90:2294-2651), one warp per measured receiver: window pick (first maximum
+// of |Re acc| over the search range, window loc -+ halftime, not clipped), then COMPUTE_TT
+// (driver.f90:855-890) on the window: the cross-correlation cc(i) = dt sum u0(k) u(k + i) for
+// lags i in (-n, n), its first maximum, and the vertex of the parabola through the three samples
+// around it.  tau = NaN marks a receiver that is not measured: a window leaving the record or a
+// peak at the end of the lag range (the reference reads past its arrays there).
+__global__ void __launch_bounds__(TT_THREADS) tt_cc_kernel(TTRow *rows, int nrows, const double2 *acc,
+                                                           const double2 *dat, int nt, int nx, int halftime,
+                                                           int given, double dt_min)
+{
+    const int warp = (blockIdx.x * TT_THREADS + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nrows) return;
+    TTRow r = rows[warp];
+    const size_t base = (size_t)r.b * nt * nx + r.x;
+    auto re = [&](const double2 *f, int t0) { return f[base + (size_t)t0 * nx].x; };  // 0-based record index
+    if (!given) {
+        const int a = max(r.timest, 1), e = min(r.timefin, nt);  // 1-based, clipped
+        double best = -1.0;
+        int bi = a;
+        for (int t = a + lane; t <= e; t += WARP) {
+            const double v = fabs(re(acc, t - 1));
+            if (v > best) { best = v; bi = t; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        r.loc = bi;
+        r.lef = bi - halftime;
+        r.rig = bi + halftime;
+    }
+    double tau = nan("");
+    if (r.lef >= 1 && r.rig <= nt && r.rig >= r.lef) {
+        const int n = r.rig - r.lef + 1, w0 = r.lef - 1;  // window sample k (1..n) is record w0 + k - 1
+        // cc at lag i = j - (n - 1): dt sum_k u0(k - min(i, 0)) u(k + max(i, 0)) over the overlap
+        auto cc = [&](int j) {
+            const int i = j - (n - 1);
+            double c = 0.0;
+            if (i <= 0) {
+                for (int k = 1; k <= n + i; k++) c += re(acc, w0 + k - i - 1) * re(dat, w0 + k - 1);
+            } else {
+                for (int k = 1; k <= n - i; k++) c += re(acc, w0 + k - 1) * re(dat, w0 + k + i - 1);
+            }
+            return c * dt_min;
+        };
+        double best = -INFINITY;
+        int bl = 2 * n;
+        for (int j = lane; j <= 2 * n - 2; j += WARP) {
+            const double c = cc(j);
+            if (c > best) { best = c; bl = j; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bl, o);
+            if (ob > best || (ob == best && oi < bl)) { best = ob; bl = oi; }
+        }
+        if (bl > 0 && bl < 2 * n - 2) {
+            const double cm = cc(bl - 1), c0 = cc(bl), cp = cc(bl + 1);
+            const double t0 = (double)(bl - (n - 1)) * dt_min;
+            // parabola c = p0 + p1 t + p2 t^2 through (t0 - dt, t0, t0 + dt); tau = -p1 / (2 p2)
+            const double p2 = (cm - 2.0 * c0 + cp) / (2.0 * dt_min * dt_min);
+            const double p1 = (cp - cm) / (2.0 * dt_min) - 2.0 * p2 * t0;
+            tau = -p1 * 0.5 / p2;
+        }
+    }
+    if (lane == 0) {
+        r.tau = tau;
+        rows[warp] = r;
+    }
+}
+
 // c(x_i, t) = con_i w_i(t) ccdot(x_i, t) at the measured receivers (the buffer is zeroed first).
 __global__ void __launch_bounds__(TT_THREADS) tt_scatter_kernel(const TTRow *rows, int nrows, const double2 *ccdot,
                                                                 double2 *c, int nt, int nx)
@@ -470,6 +544,49 @@ int sparc_tt_mode(sparc_tt_plan_t *p, const double *filter, int nrows, int *rows
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return tt_fail("sparc_tt_mode", e);
+    for (int r = 0; r < nrows; r++) {
+        int *q = rows + 7 * r;
+        q[4] = h[r].lef;
+        q[5] = h[r].rig;
+        q[6] = h[r].loc;
+        tau[r] = h[r].tau;
+    }
+    return SPARC_OK;
+}
+
+int sparc_tt_misfit_mode(sparc_tt_plan_t *p, const double *filter, int nrows, int *rows, int halftime, int given,
+                         double dt_min, double *tau, void *stream)
+{
+    if (!p || !filter || nrows < 0 || nrows > p->cap || (nrows > 0 && (!rows || !tau)) || halftime < 0)
+        return report_error(SPARC_ERR_ARG, "sparc_tt_misfit_mode: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nt = p->nt, nx = p->nx;
+    const long long n = (long long)p->nb * nt * nx;
+    std::vector<TTRow> h(nrows);
+    for (int r = 0; r < nrows; r++) {
+        const int *q = rows + 7 * r;
+        if (q[0] < 0 || q[0] >= p->nb || q[1] < 0 || q[1] >= nx)
+            return report_error(SPARC_ERR_ARG, "sparc_tt_misfit_mode: row out of range");
+        if (!given && (max(q[2], 1) > min(q[3], nt)))
+            return report_error(SPARC_ERR_ARG, "sparc_tt_misfit_mode: empty search range");
+        h[r] = TTRow{q[0], q[1], q[2], q[3], q[4], q[5], 0, 0, 0.0, 0.0};
+    }
+    tt_filter_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->S, p->ACC, filter, nt, nx, n, 0, dt_min);
+    tt_filter_kernel<<<tt_grid(n), TT_THREADS, 0, st>>>(p->D, p->DAT, filter, nt, nx, n, 0, dt_min);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = dft2(p, p->ACC, 1, st);
+    if (e == cudaSuccess) e = dft2(p, p->DAT, 1, st);
+    if (e == cudaSuccess && nrows > 0) {
+        e = cudaMemcpyAsync(p->rows, h.data(), nrows * sizeof(TTRow), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            const unsigned g = (unsigned)(((long long)nrows * WARP + TT_THREADS - 1) / TT_THREADS);
+            tt_cc_kernel<<<g, TT_THREADS, 0, st>>>(p->rows, nrows, p->ACC, p->DAT, nt, nx, halftime, given, dt_min);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), p->rows, nrows * sizeof(TTRow), cudaMemcpyDeviceToHost, st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return tt_fail("sparc_tt_misfit_mode", e);
     for (int r = 0; r < nrows; r++) {
         int *q = rows + 7 * r;
         q[4] = h[r].lef;

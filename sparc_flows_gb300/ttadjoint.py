@@ -140,6 +140,19 @@ def read_measurement_files(directory: str):
     return modes, freq
 
 
+BANDS = [(2.0, 3.5), (3.5, 4.5), (4.5, 6.0)]  # MISFIT_ALL's frequency bands, driver.f90:2376-2385
+
+
+def misfit_search_range(pord: int, dist: float, dt_min: float) -> tuple[int, int]:
+    """timest, timefin of MISFIT_ALL's window pick (driver.f90:2436-2446): the f/p modes as in
+    ADJOINT_SOURCE_FILT, the first bounce (pord 8) with its own polynomials."""
+    if pord != 8:
+        return search_range(pord, dist, dt_min)
+    ts = math.floor((_f(-1.45511095e-04) * dist ** 2 + _f(2.72140632e-01) * dist + _f(2.16331969e+01)) * (1.0 / dt_min))
+    tf = math.floor((_f(3.85746516e-08) * dist ** 2 + _f(2.21324786e-01) * dist + _f(4.36702155e+01)) * (1.0 / dt_min))
+    return ts, tf
+
+
 def search_range(pord: int, dist: float, dt_min: float) -> tuple[int, int]:
     """timest, timefin of the window pick (driver.f90:2046-2053), 1-based."""
     if pord != 8:
@@ -226,6 +239,57 @@ class TTAdjoint:
         torch.cuda.current_stream(self.dev).synchronize()
         return {"adj": adj, "misfit": 0.5 * misfit, "nmeas": nmeas, "rows": rows_out, "windows": wins_out}
 
+    def misfit_all(self, synth, data, x00s, t_min: np.ndarray, modes: dict, windows: dict | None = None):
+        """MISFIT_ALL (driver.f90:2294-2651): cross-correlation travel times of every ridge filter
+        in three frequency bands.  windows {band (1..3): {pord: {b: [(lef, rig), ...]}}} to reuse.
+        Returns a list over the bands of dict(band, nmeas (nb, 11), misfit (nb, 11) halved,
+        windows {pord: {b: [(lef, rig)]}} as picked (unclipped))."""
+        nb, nt, nx = self.nb, self.nt, self.nx
+        s = torch.as_tensor(synth, dtype=torch.float64, device=self.dev).contiguous()
+        d = torch.as_tensor(data, dtype=torch.float64, device=self.dev).contiguous()
+        capi.check(self.L.sparc_tt_set_records(self.plan, s.data_ptr(), d.data_ptr(), self._stream()),
+                   "sparc_tt_set_records")
+        dt = float(t_min[1] - t_min[0])
+        ridges = ridge_filters(nx, nt, self.xlength_cm, self.outputcad)
+        out = []
+        for fb, (left, right) in enumerate(BANDS, start=1):
+            ff = freq_filter(left, right, nt, self.outputcad)
+            nmeas = np.zeros((nb, 11), dtype=int)
+            mis = np.zeros((nb, 11))
+            wins = {}
+            for pord in sorted(modes):
+                mindist, maxdist, window = modes[pord]
+                halftime = int(math.floor(window / (2.0 * dt) + 0.5))
+                given = windows is not None and fb in windows and pord in windows[fb]
+                rows = []
+                for b in range(nb):
+                    dist = self.distances(x00s[b])
+                    it = iter(windows[fb][pord].get(b, [])) if given else None
+                    for i in range(nx):
+                        if not (dist[i] > mindist and dist[i] < maxdist):
+                            continue
+                        ts, tf = misfit_search_range(pord, dist[i], dt)
+                        lef, rig = next(it) if given else (0, 0)
+                        if not given and max(ts, 1) > min(tf, nt):
+                            continue
+                        rows.append((b, i, ts, tf, lef, rig, 0))
+                arr = np.ascontiguousarray(np.array(rows, dtype=np.int32).reshape(-1, 7))
+                tau = np.zeros(max(len(rows), 1))
+                filt = torch.as_tensor(ridges[pord] * ff[:, None], dtype=torch.float64, device=self.dev).contiguous()
+                capi.check(self.L.sparc_tt_misfit_mode(self.plan, filt.data_ptr(), len(rows),
+                                                       arr.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), halftime,
+                                                       int(given), dt, tau.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                       self._stream()), "sparc_tt_misfit_mode")
+                per_w = {}
+                for r, (b, i, ts, tf, lef, rig, loc) in enumerate(arr.tolist()):
+                    per_w.setdefault(b, []).append((lef, rig))
+                    if np.isfinite(tau[r]):
+                        mis[b, pord] += tau[r] ** 2
+                        nmeas[b, pord] += 1
+                wins[pord] = per_w
+            out.append({"band": (left, right), "nmeas": nmeas, "misfit": 0.5 * mis, "windows": wins})
+        return out
+
     def close(self):
         if getattr(self, "plan", None):
             self.L.sparc_tt_plan_destroy(self.plan)
@@ -270,6 +334,40 @@ def write_outputs(directory: str, contrib: str, jobno: str, res: dict, b: int, t
     os.makedirs(kdir, exist_ok=True)
     with open(os.path.join(kdir, f"misfit_{contrib}_{jobno}"), "w") as fh:
         fh.write(f"{int(contrib):12d}{int(res['nmeas'][b]):12d}  {float(res['misfit'][b])!r}\n")
+
+
+def write_misfit_all(directory: str, contrib: str, jobno: str, bands: list, b: int, linesearch: bool):
+    """kernel/misfit_all_NN_MM (three blocks of '# NN left right', '# nmeas(0:10)', misfit(0:10)/2)
+    and, outside line searches, forward_srcNN_ls00/windows.all.<pord 2 digits>.<band>
+    (driver.f90:2361-2362, 2420-2432, 2470-2476)."""
+    kdir = os.path.join(directory, "kernel")
+    os.makedirs(kdir, exist_ok=True)
+    with open(os.path.join(kdir, f"misfit_all_{contrib}_{jobno}"), "w") as fh:
+        for bd in bands:
+            left, right = bd["band"]
+            fh.write(f" # {int(contrib):12d} {left!r} {right!r}\n")
+            fh.write(" # " + " ".join(f"{int(v):12d}" for v in bd["nmeas"][b]) + "\n")
+            fh.write(" " + " ".join(repr(float(v)) for v in bd["misfit"][b]) + "\n")
+    if not linesearch:
+        wdir = os.path.join(directory, f"forward_src{contrib}_ls00")
+        os.makedirs(wdir, exist_ok=True)
+        for fb, bd in enumerate(bands, start=1):
+            for pord, per_b in bd["windows"].items():
+                with open(os.path.join(wdir, f"windows.all.{pord:02d}.{fb}"), "w") as fh:
+                    for (lef, rig) in per_b.get(b, []):
+                        fh.write(f"{lef:12d}{rig:12d}\n")
+
+
+def read_windows_all(directory: str, contrib: str, modes: dict) -> dict:
+    """windows.all.<pord>.<band> of the ls00 forward run (read back in line searches)."""
+    out = {}
+    for fb in (1, 2, 3):
+        for pord in modes:
+            f = os.path.join(directory, f"forward_src{contrib}_ls00", f"windows.all.{pord:02d}.{fb}")
+            if os.path.exists(f):
+                vals = np.loadtxt(f, dtype=int, ndmin=2)
+                out.setdefault(fb, {})[pord] = {0: [tuple(map(int, v)) for v in vals]}
+    return out
 
 
 def read_windows(directory: str, contrib: str, modes: dict) -> dict:

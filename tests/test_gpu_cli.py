@@ -116,6 +116,9 @@ def test_forward_writes_the_travel_time_adjoint_source(tmp_path):
     assert int(info[0]) == nsteps // 15 + 1 and info[-1] == "2D"
     mis = np.loadtxt(data / "kernel" / "misfit_02_00")
     assert int(mis[0]) == 2 and int(mis[1]) == rows.shape[0] and mis[2] > 0
+    lines = (data / "kernel" / "misfit_all_02_00").read_text().splitlines()
+    assert len(lines) == 9 and lines[0].split()[:2] == ["#", "2"]
+    assert all((data / "forward_src02_ls00" / f"windows.all.00.{fb}").exists() for fb in (1, 2, 3))
 
 
 def test_unknown_source_fails_with_nonzero_status(tmp_path):

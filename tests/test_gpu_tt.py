@@ -59,3 +59,26 @@ def test_no_measurement_gives_zero_source():
     res = tt.run(torch.as_tensor(s, device="cuda"), torch.as_tensor(d, device="cuda"), X00, _tmin(), {})
     assert (res["adj"] == 0).all() and (res["nmeas"] == 0).all()
     tt.close()
+
+
+def test_misfit_all_matches_oracle():
+    s, d = _records(2)
+    tt = TT.TTAdjoint(NX, NT, len(X00), XL, CAD)
+    bands = tt.misfit_all(torch.as_tensor(s, device="cuda"), torch.as_tensor(d, device="cuda"), X00, _tmin(), MODES)
+    assert len(bands) == 3
+    for b, x00 in enumerate(X00):
+        ref = TO.misfit_all(s[b], d[b], x00, XL, _tmin(), CAD, MODES)
+        for fb in range(3):
+            assert bands[fb]["band"] == ref[fb]["band"]
+            assert np.array_equal(bands[fb]["nmeas"][b], ref[fb]["nmeas"])
+            assert np.allclose(bands[fb]["misfit"][b], ref[fb]["misfit"], rtol=1e-9, atol=0)
+            for pord in MODES:
+                assert bands[fb]["windows"][pord].get(b, []) == ref[fb]["windows"][pord]
+    assert sum(int(bd["nmeas"].sum()) for bd in bands) > 0
+    # line search: the picked windows given back reproduce the misfits
+    given = {fb + 1: bands[fb]["windows"] for fb in range(3)}
+    again = tt.misfit_all(torch.as_tensor(s, device="cuda"), torch.as_tensor(d, device="cuda"), X00, _tmin(), MODES,
+                          windows=given)
+    for fb in range(3):
+        assert np.allclose(again[fb]["misfit"], bands[fb]["misfit"], rtol=1e-12)
+    tt.close()

@@ -52,3 +52,18 @@ def test_measurement_files(tmp_path):
     modes, freq = TT.read_measurement_files(str(tmp_path))
     assert modes == {0: (5.0, 40.0, 12.5), 8: (10.0, 60.0, 20.0)}
     assert freq == {"allmodes": (1.5, 5.5)}
+
+
+def test_misfit_search_ranges_match_oracle():
+    for pord in range(9):
+        for dist in (3.7, 12.0, 25.5, 55.0):
+            assert TT.misfit_search_range(pord, dist, 0.5) == TO.misfit_search_range(pord, dist, 0.5)
+
+
+def test_compute_tt_of_a_shifted_pulse():
+    """A Gaussian pulse delayed by 0.8 records: COMPUTE_TT returns the delay (positive = late)."""
+    t = np.arange(41, dtype=float)
+    u0 = np.exp(-((t - 20.0) / 3.0) ** 2)
+    u = np.exp(-((t - 20.8) / 3.0) ** 2)
+    tau = TO.compute_tt(u0, u, 0.5)
+    assert abs(tau - 0.4) < 0.02
