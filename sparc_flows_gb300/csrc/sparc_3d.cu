@@ -32,6 +32,11 @@ constexpr int S3_THREADS = 256;
 // (64 bytes in FP32) of one y-row.
 constexpr int DDY_COLS = 16;
 constexpr int DDY_WARPS = DDY_COLS / 2;
+// Per-warp region of the shared-memory transform: xr, xi, yr, yi of NY values each, every array
+// offset by one more word and the regions DDY_SPAN(NY) words apart (not a multiple of 32), so
+// that the 16 columns a warp scatters on load (and gathers on store) fall in different banks.
+template <int NY>
+constexpr int ddy_span() { return 4 * NY + 5; }
 
 template <typename T, int NY>
 __global__ void __launch_bounds__(DDY_WARPS *WARP) ddy_kernel(const T *__restrict__ var, T *__restrict__ dvar,
@@ -40,18 +45,19 @@ __global__ void __launch_bounds__(DDY_WARPS *WARP) ddy_kernel(const T *__restric
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = reinterpret_cast<T *>(smem_raw);
+    constexpr int S = ddy_span<NY>();
     __shared__ T s_inv[DDY_COLS];
-    __shared__ int s_out_x[DDY_WARPS];  // 0: result in the warp's first buffer pair, 1: second
+    __shared__ int s_off[DDY_WARPS][2];  // offsets of the result arrays in each warp's region
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t plane = (size_t)blockIdx.y * NY * nx;
     const int x0 = blockIdx.x * DDY_COLS;
     for (int idx = threadIdx.x; idx < NY * DDY_COLS; idx += DDY_WARPS * WARP) {
         const int y = idx / DDY_COLS, c = idx % DDY_COLS;
-        T *w = sm + (size_t)(c >> 1) * 4 * NY;
-        w[(c & 1) * NY + y] = var[plane + (size_t)y * nx + x0 + c];
+        sm[(c >> 1) * S + (c & 1) * (NY + 1) + y] = var[plane + (size_t)y * nx + x0 + c];
     }
     __syncthreads();
-    T *xr = sm + (size_t)warp * 4 * NY, *xi = xr + NY, *yr = xi + NY, *yi = yr + NY;
+    T *base = sm + warp * S;
+    T *xr = base, *xi = base + (NY + 1), *yr = base + 2 * (NY + 1), *yi = base + 3 * (NY + 1);
     T mr = T(0), mi = T(0);
     for (int y = lane; y < NY; y += WARP) {
         mr = fmax(mr, fabs(xr[y]));
@@ -65,13 +71,13 @@ __global__ void __launch_bounds__(DDY_WARPS *WARP) ddy_kernel(const T *__restric
     if (lane == 0) {
         s_inv[2 * warp] = isr;
         s_inv[2 * warp + 1] = isi;
-        s_out_x[warp] = (orr == xr) ? 0 : 1;
+        s_off[warp][0] = (int)(orr - base);
+        s_off[warp][1] = (int)(oi - base);
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < NY * DDY_COLS; idx += DDY_WARPS * WARP) {
         const int y = idx / DDY_COLS, c = idx % DDY_COLS, w = c >> 1;
-        const T *res = sm + (size_t)w * 4 * NY + (size_t)s_out_x[w] * 2 * NY + (c & 1) * NY;
-        dvar[plane + (size_t)y * nx + x0 + c] = res[y] * s_inv[c];
+        dvar[plane + (size_t)y * nx + x0 + c] = sm[w * S + s_off[w][c & 1] + y] * s_inv[c];
     }
 }
 
@@ -79,7 +85,7 @@ template <typename T, int NY>
 static cudaError_t ddy_n(const T *var, T *dvar, int nplanes, int nx, T stretchy, const T *twr, const T *twi,
                          const T *kap, cudaStream_t st)
 {
-    const size_t smem = (size_t)DDY_WARPS * 4 * NY * sizeof(T);
+    const size_t smem = (size_t)DDY_WARPS * ddy_span<NY>() * sizeof(T);
     auto k = ddy_kernel<T, NY>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -617,6 +617,10 @@ cudaError_t launch_ddz(const ZTab<T> &tb, int nch, int L, const T *var, T *dvar,
                        const T *stretch, int filter, cudaStream_t st)
 {
     if (L > ColCfg<T>::LMAX || nch > ColCfg<T>::MAXNCH || n1 <= 0) return cudaErrorInvalidValue;
+    // many columns (a 3-D field: nb * ny * nx): 32 columns per block, four 32-byte sectors per
+    // row access; few (a 2-D row of nx): 8, so that enough blocks exist
+    if (n1 % 32 == 0 && n1 >= 32 * 152 * 8)
+        return launch_ddz_cw<T, 32>(tb, nch, L, var, dvar, n1, nz, preset, stretch, filter, st);
     return launch_ddz_cw<T, 8>(tb, nch, L, var, dvar, n1, nz, preset, stretch, filter, st);
 }
 
