@@ -37,13 +37,15 @@ class FwdAdjKernels:
     """Batched forward + adjoint + kernel computation for one model and many sources."""
 
     def __init__(self, run: RunConfig, model: np.ndarray, specs: list[SourceSpec], psi=None, cmul=None,
-                 precision: int = 32, receivers: np.ndarray | None = None, device: str = "cuda:0"):
+                 precision: int = 32, receivers: np.ndarray | None = None, device: str = "cuda:0",
+                 column_impl: int | None = None, column_block: int | None = None):
         self.run, self.nb = run, len(specs)
         self.dev = torch.device(device)
-        self.fwd = WaveSolver(run, model, nbatch=self.nb, precision=precision, cmul=cmul, psi=psi, device=device)
+        col = dict(column_impl=column_impl, column_block=column_block)
+        self.fwd = WaveSolver(run, model, nbatch=self.nb, precision=precision, cmul=cmul, psi=psi, device=device, **col)
         self.fwd.set_forward_sources(specs)
         self.adj = WaveSolver(run.replace(adjoint=True), model, nbatch=self.nb, precision=precision, cmul=cmul,
-                              psi=psi, device=device)
+                              psi=psi, device=device, **col)
         self.nrec = run.nrec
         self.rcv = receiver_columns(run) if receivers is None else np.asarray(receivers)
         dt = self.fwd.dtype

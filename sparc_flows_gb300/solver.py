@@ -69,10 +69,11 @@ class WaveSolver:
     """
 
     def __init__(self, run: RunConfig, model: np.ndarray, nbatch: int = 1, precision: int = 64, cmul=None,
-                 psi=None, device: str = "cuda:0"):
+                 psi=None, device: str = "cuda:0", column_impl: int | None = None, column_block: int | None = None):
         if not torch.cuda.is_available():
             raise capi.SparcError("WaveSolver needs a CUDA device")
         self.run, self.nb, self.precision = run, nbatch, precision
+        self._column = (column_impl, column_block)
         self.dev = torch.device(device)
         self.dtype = torch.float32 if precision == 32 else torch.float64
         nx, nz = run.nx, run.nz
@@ -125,8 +126,9 @@ class WaveSolver:
         cfg.steps_out, cfg.k_inj, cfg.k_obs, cfg.src_until = run.steps_out, k_inj, self.o_rad, run.src_until
         cfg.filter_k0, cfg.filter_all_x = run.filter_kst - 1, int(run.filter_all_x)
         cfg.compensated = int(os.environ.get("SPARC_COMPENSATED", "0"))
-        cfg.column_impl = int(os.environ.get("SPARC_COLUMN_IMPL", "2"))
-        cfg.column_block = int(os.environ.get("SPARC_COLUMN_BLOCK", "32"))
+        impl, block = self._column
+        cfg.column_impl = int(os.environ.get("SPARC_COLUMN_IMPL", "2")) if impl is None else int(impl)
+        cfg.column_block = int(os.environ.get("SPARC_COLUMN_BLOCK", "32")) if block is None else int(block)
         self.cfg = cfg
         h = ctypes.c_void_p()
         capi.check(self.L.sparc_plan_create(ctypes.byref(cfg), ctypes.byref(h)), "sparc_plan_create")

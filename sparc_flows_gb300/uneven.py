@@ -2,7 +2,8 @@
 
 Solves sharing (nx, steps) form one batched plan (per-solve stream function and sound-speed
 multiplier, a per-solve background in HBM); the groups run concurrently, each from its own host
-thread on its own CUDA stream, so that small groups fill the GPU together.  The reference runs
+thread on its own CUDA stream, so that small groups fill the GPU together.  Each group's
+column-pass variant is chosen by timing the candidates on that group's own plan (autotune).  The reference runs
 every solve as its own single-rank ``sparc`` process (data_forward.sh:28).
 """
 from __future__ import annotations
@@ -24,12 +25,39 @@ def group_solves(solves: list) -> dict:
     return groups
 
 
+# column-pass variants an autotuned plan chooses from: (column_impl, column_block)
+COLUMN_CANDIDATES = {32: [(2, 32), (2, 16), (2, 8), (3, 8), (0, 32), (0, 8), (1, 8)],
+                     64: [(0, 32), (0, 8), (1, 8)]}
+
+
+def autotune_column(run, model, specs, psi, cmul, precision: int, device, nsteps: int = 8,
+                    candidates=None) -> tuple[tuple[int, int], dict]:
+    """Fastest column-pass variant for one group: each candidate plan (same grid, batch and
+    backgrounds) is stepped nsteps times after a warm-up and timed per pass with CUDA events
+    (sparc_profile_passes); the variant with the least time per step wins.  Returns
+    ((column_impl, column_block), {candidate: ms per step})."""
+    from .solver import WaveSolver
+
+    cands = candidates or COLUMN_CANDIDATES[precision]
+    times = {}
+    for impl, block in cands:
+        ws = WaveSolver(run, model, nbatch=len(specs), precision=precision, cmul=cmul, psi=psi, device=device,
+                        column_impl=impl, column_block=block)
+        ws.set_forward_sources(specs)
+        ws.profile_passes(nsteps=2)
+        p = ws.profile_passes(nsteps=nsteps)
+        times[(impl, block)] = sum(p["per_class_ms"].values())
+        ws.close()
+    best = min(times, key=times.get)
+    return best, times
+
+
 class UnevenBatch:
-    def __init__(self, solves: list, precision: int = 32, device: str = "cuda:0"):
+    def __init__(self, solves: list, precision: int = 32, device: str = "cuda:0", autotune: bool = True):
         self.solves, self.dev = solves, torch.device(device)
         model = M.polytrope(300)
         self.groups = group_solves(solves)
-        self.pipes, self.streams = {}, {}
+        self.pipes, self.streams, self.tuned = {}, {}, {}
         for key, idx in self.groups.items():
             nx, nsteps = key
             run = M.uneven_run(nx, nsteps)
@@ -41,8 +69,13 @@ class UnevenBatch:
                 specs.append(M.SourceSpec(s.xloc))
             half = 0.45 * nx * 0.78125
             rcv = receiver_columns(run, n=int(2 * half / 2.0), x0=-half, dx=2.0)
+            col = {}
+            if autotune:
+                best, times = autotune_column(run, model, specs, psis, cmuls, precision, device)
+                self.tuned[key] = {"choice": best, "ms_per_step": {f"{i},{b}": t for (i, b), t in times.items()}}
+                col = dict(column_impl=best[0], column_block=best[1])
             self.pipes[key] = FwdAdjKernels(run, model, specs, psi=psis, cmul=cmuls, precision=precision,
-                                            receivers=rcv, device=device)
+                                            receivers=rcv, device=device, **col)
             self.streams[key] = torch.cuda.Stream(device=self.dev)
 
     def point_steps(self) -> int:
