@@ -290,6 +290,16 @@ int sparc_tt_misfit_mode(sparc_tt_plan_t *plan, const double *filter, int nrows,
 int sparc_tt_adjoint(sparc_tt_plan_t *plan, double *adj, void *stream);
 
 /* ---------------------------------------------------------------------------------------------
+ * FITS payloads on the device: n values of a device array (FP32 or FP64) to / from the
+ * big-endian IEEE payload of a FITS primary array (BITPIX -64 or -32), device to device.  The
+ * partial-state files of the reference's forward / adjoint runs and kernel stage
+ * (WRITE_OUT_PARTIAL_STATE all_modules.f90:750-784, readfits kernels.f90:221-280, writefits /
+ * readfits all_modules.f90:99-378) are these payloads behind a 2880-byte header.
+ * ------------------------------------------------------------------------------------------- */
+int sparc_fits_encode(const void *src, int precision, long long n, int bitpix, void *dst, void *stream);
+int sparc_fits_decode(const void *src, int bitpix, long long n, void *dst, int precision, void *stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Gradient post-processing (replaces grad.py's array work, grad.py:42-117, 188-364).  Every
  * array is FP64 on the device, x-fastest [nz][nx] as the kernels above; no call allocates: the
  * caller passes a workspace of sparc_grad_workspace_bytes(nx, nz) bytes (the vector calls need

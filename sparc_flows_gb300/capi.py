@@ -59,6 +59,8 @@ SIGNATURES = {
     "sparc_tt_misfit_mode": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_double, _dp, _vp]),
     "sparc_tt_adjoint": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc_fits_encode": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_longlong, ctypes.c_int, _vp, _vp]),
+    "sparc_fits_decode": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_longlong, _vp, ctypes.c_int, _vp]),
     "sparc_grad_workspace_bytes": (ctypes.c_ulonglong, [ctypes.c_int, ctypes.c_int]),
     "sparc_gradient": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sparc_vec_dot": (ctypes.c_int, [ctypes.c_longlong, _vp, _vp, _vp, _dp, _vp, _vp]),

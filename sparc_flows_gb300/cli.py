@@ -16,7 +16,9 @@ Files written (same names and FITS layout as the reference):
   <dir>/kernel/{kernel_c_NN, kernel_vx_NN, kernel_vz_NN, kernel_psi_NN, hessian_NN}.fits
 The partial states the reference dumps every 15 steps as ~3000 FITS files
 (all_modules.f90:750-784) are kept as one array file per run (partial_states.npy) in the same
-folders and removed by the kernel stage, as PRODUCE_KERNELS removes its *partial* files.
+folders, or with SPARC_PARTIAL_FITS=1 written as the reference's own *_partial.fits files
+(payloads encoded on the GPU); the kernel stage reads either, so it also consumes partial
+states written by the reference, and removes them as PRODUCE_KERNELS does.
 
 Adjoint source: a forward run that is not a data run computes the travel-time adjoint source
 of ADJOINT_SOURCE_FILT (driver.f90:1758-2238; ttadjoint.py, csrc/sparc_tt.cu) from the ridge
@@ -26,7 +28,7 @@ forward_srcNN_ls00/windows.<pord> and kernel/misfit_NN_MM; SPARC_ADJOINT_SOURCE=
 writes the time-reversed waveform residual (synthetic minus <dir>/data/NN.fits) instead.
 
 Environment: SPARC_PRECISION (64, or 32), SPARC_DEVICE (cuda:0), SPARC_NSTEPS (override maxtime+1),
-SPARC_ADJOINT_SOURCE (tt, or waveform).
+SPARC_ADJOINT_SOURCE (tt, or waveform), SPARC_PARTIAL_FITS (0, or 1).
 """
 from __future__ import annotations
 
@@ -134,7 +136,7 @@ def _forward(run, model, directory, contrib, jobno, src, precision, device, comp
     with open(os.path.join(out, "rms_hist"), "w") as f:
         f.write(f"{float(np.sqrt((s[-1] ** 2).sum()))}\n")
     if keep:
-        np.save(os.path.join(out, "partial_states.npy"), snaps.cpu().numpy()[0])
+        _save_partial_states(out, snaps[0], run.steps_out, forward=True)
     if not compute_data:
         data_p = os.path.join(directory, "data", f"{contrib}.fits")
         data = fits.read(data_p).reshape(s.shape) if os.path.exists(data_p) else np.zeros_like(s)
@@ -183,7 +185,7 @@ def _adjoint(run, model, directory, contrib, jobno, precision, device):
     vr = fits.read(srcf).reshape(-1, run.nx)[: run.forcing_length]
     ws.set_adjoint_sources(vr[None])
     _, snaps = ws.forward(snapshots=True)
-    np.save(os.path.join(adir, "partial_states.npy"), snaps.cpu().numpy()[0])
+    _save_partial_states(adir, snaps[0], run.steps_out, forward=False)
     with open(os.path.join(adir, "kernel_info"), "w") as f:
         f.write(f"{run.forcing_length}\n{((run.nsteps - 1) // run.cadforcing_step) * run.cadforcing_step}\n")
     ws.close()
@@ -197,20 +199,76 @@ def _kernels(run, model, directory, contrib, jobno, precision, device):
 
     fdir = os.path.join(directory, f"forward_src{contrib}_ls{jobno}")
     adir = os.path.join(directory, f"adjoint_src{contrib}")
-    fp, ap = os.path.join(fdir, "partial_states.npy"), os.path.join(adir, "partial_states.npy")
-    if not (os.path.exists(fp) and os.path.exists(ap)):
-        print("sparc: partial states of the forward and adjoint runs are missing", file=sys.stderr)
-        return 1
     ws = _solver(run, model, directory, jobno, precision, device, False)
-    ker = kernels_from_partial_states(ws, np.load(fp), np.load(ap))
+    fsn = _load_partial_states(fdir, True, ws)
+    asn = _load_partial_states(adir, False, ws)
+    if fsn is None or asn is None:
+        print("sparc: partial states of the forward and adjoint runs are missing", file=sys.stderr)
+        ws.close()
+        return 1
+    ker = kernels_from_partial_states(ws, fsn, asn)
     kdir = os.path.join(directory, "kernel")
     os.makedirs(kdir, exist_ok=True)
     for name in ("kernel_c", "kernel_vx", "kernel_vz", "kernel_psi", "hessian"):
         fits.write(os.path.join(kdir, f"{name}_{contrib}.fits"), ker[name][:, None, :])
-    os.remove(fp)
-    os.remove(ap)
+    for d in (fdir, adir):  # kernels.f90:593-595 removes the partial states
+        for f in os.listdir(d):
+            if f == "partial_states.npy" or f.endswith("_partial.fits"):
+                os.remove(os.path.join(d, f))
     ws.close()
     return 0
+
+
+# partial-state fields of the reference's files (all_modules.f90:759-775) and their slot in the
+# (6, nz, nx) records of this package: xi_x, xi_z, v_x, v_z, acc_x, acc_z
+_PARTIAL_FWD = (("xix", 0), ("xiz", 1), ("vx", 2), ("vz", 3), ("acc_x", 4), ("acc_z", 5))
+_PARTIAL_ADJ = (("vx", 2), ("vz", 3), ("acc_x", 4), ("acc_z", 5))
+
+
+def _save_partial_states(d, snaps, steps_out, forward):
+    """Partial states of a run: one array file, or with SPARC_PARTIAL_FITS=1 the reference's
+    files {xix, xiz (forward only), vx, vz, acc_x, acc_z}_<6-digit step>_partial.fits
+    (WRITE_OUT_PARTIAL_STATE, all_modules.f90:750-784), encoded on the GPU."""
+    if os.environ.get("SPARC_PARTIAL_FITS", "0") != "1":
+        np.save(os.path.join(d, "partial_states.npy"), snaps.cpu().numpy())
+        return
+    from .fits_gpu import write_fields
+
+    nrec, _, nz, nx = snaps.shape
+    names = _PARTIAL_FWD if forward else _PARTIAL_ADJ
+    for r in range(nrec):
+        t = r * steps_out
+        write_fields([os.path.join(d, f"{nm}_{t:06d}_partial.fits") for nm, _ in names],
+                     snaps[r, [j for _, j in names]], shape=(nz, 1, nx))
+
+
+def _load_partial_states(d, forward, ws):
+    """(nrec, 6, nz, nx) partial states of a run directory from partial_states.npy or from the
+    reference's partial-state FITS files (read as kernels.f90:221-280 reads them, decoded on
+    the GPU; fields an adjoint run does not write stay zero).  None when neither exists."""
+    import torch
+
+    npy = os.path.join(d, "partial_states.npy")
+    if os.path.exists(npy):
+        return np.load(npy)
+    if not os.path.isdir(d):
+        return None
+    times = sorted(int(f[4:10]) for f in os.listdir(d) if f.startswith("vz_") and f.endswith("_partial.fits"))
+    if not times:
+        return None
+    from .fits_gpu import read_fields
+
+    names = _PARTIAL_FWD if forward else _PARTIAL_ADJ
+    out = None
+    for r, t in enumerate(times):
+        flds = read_fields([os.path.join(d, f"{nm}_{t:06d}_partial.fits") for nm, _ in names], ws.dev,
+                           precision=ws.precision)
+        if out is None:
+            nz, nx = flds.shape[1], flds.shape[-1]
+            out = torch.zeros((len(times), 6, nz, nx), dtype=flds.dtype, device=ws.dev)
+        for i, (_, j) in enumerate(names):
+            out[r, j] = flds[i].reshape(nz, nx)
+    return out
 
 
 if __name__ == "__main__":

@@ -30,30 +30,37 @@ def _card(key: str, value=None, comment: str = "") -> bytes:
     return s[:80].ljust(80).encode("ascii")
 
 
-def write(path: str, data, time: int | None = None) -> None:
-    """Write a 1..3-D array (NumPy order) as a BITPIX=-64 primary HDU."""
-    a = np.asarray(data, dtype=">f8")
-    shape = a.shape[::-1]  # FITS NAXIS1 is the fastest axis
-    cards = [_card("SIMPLE", True), _card("BITPIX", -64), _card("NAXIS", len(shape))]
-    for i, n in enumerate(shape, 1):
+def header(shape: tuple, time: int | None = None, bitpix: int = -64) -> bytes:
+    """Primary header of an array of NumPy shape `shape`, padded to a 2880-byte block."""
+    dims = tuple(shape)[::-1]  # FITS NAXIS1 is the fastest axis
+    cards = [_card("SIMPLE", True), _card("BITPIX", bitpix), _card("NAXIS", len(dims))]
+    for i, n in enumerate(dims, 1):
         cards.append(_card(f"NAXIS{i}", int(n)))
     cards.append(_card("EXTEND", False))
     if time is not None:
         cards.append(_card("TIME", int(time), "Also, init = time+1"))
     cards.append(_card("END"))
     hdr = b"".join(cards)
-    hdr += b" " * (-len(hdr) % BLOCK)
-    body = np.ascontiguousarray(a).tobytes()
-    body += b"\0" * (-len(body) % BLOCK)
+    return hdr + b" " * (-len(hdr) % BLOCK)
+
+
+def write_raw(path: str, shape: tuple, payload, time: int | None = None, bitpix: int = -64) -> None:
+    """Header plus an already encoded big-endian payload (bytes-like), zero-padded to a block."""
+    body = memoryview(payload).cast("B")
     with open(path, "wb") as f:
-        f.write(hdr)
+        f.write(header(shape, time, bitpix))
         f.write(body)
+        f.write(b"\0" * (-len(body) % BLOCK))
 
 
-def read(path: str) -> np.ndarray:
-    """Read the primary array of a FITS file (BITPIX -64, -32, 16, 32 or 64) in NumPy order."""
-    with open(path, "rb") as f:
-        raw = f.read()
+def write(path: str, data, time: int | None = None) -> None:
+    """Write a 1..3-D array (NumPy order) as a BITPIX=-64 primary HDU."""
+    a = np.ascontiguousarray(np.asarray(data, dtype=">f8"))
+    write_raw(path, a.shape, a.tobytes(), time)
+
+
+def parse_header(raw: bytes, path: str = "") -> dict:
+    """Keywords of the primary header and the payload offset (key 'offset')."""
     hdr = {}
     pos = 0
     while True:
@@ -69,14 +76,24 @@ def read(path: str) -> np.ndarray:
                 done = True
                 break
             if card[8:10] == "= ":
-                val = card[10:].split("/")[0].strip()
-                hdr[key] = val
+                hdr[key] = card[10:].split("/")[0].strip()
         if done:
             break
     bitpix = int(hdr["BITPIX"])
     naxis = int(hdr["NAXIS"])
-    shape = tuple(int(hdr[f"NAXIS{i}"]) for i in range(naxis, 0, -1))
-    dt = {-64: ">f8", -32: ">f4", 16: ">i2", 32: ">i4", 64: ">i8"}[bitpix]
+    hdr["shape"] = tuple(int(hdr[f"NAXIS{i}"]) for i in range(naxis, 0, -1))
+    hdr["bitpix"] = bitpix
+    hdr["offset"] = pos
+    return hdr
+
+
+def read(path: str) -> np.ndarray:
+    """Read the primary array of a FITS file (BITPIX -64, -32, 16, 32 or 64) in NumPy order."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    hdr = parse_header(raw, path)
+    shape, pos = hdr["shape"], hdr["offset"]
+    dt = {-64: ">f8", -32: ">f4", 16: ">i2", 32: ">i4", 64: ">i8"}[hdr["bitpix"]]
     n = int(np.prod(shape)) if shape else 0
     nbytes = n * np.dtype(dt).itemsize
     if pos + nbytes > len(raw):

@@ -82,6 +82,41 @@ def test_forward_adjoint_kernel_files(tmp_path):
     assert not (fdir / "partial_states.npy").exists()
 
 
+def test_partial_states_as_reference_fits_files(tmp_path):
+    """SPARC_PARTIAL_FITS=1: forward and adjoint runs write the reference's *_partial.fits files
+    (xix, xiz, vx, vz, acc_x, acc_z per record; v and acc only for the adjoint), the kernel stage
+    reads them and gives the kernels of the array-file path, then removes them."""
+    outs = {}
+    for mode in ("0", "1"):
+        code = tmp_path / f"code{mode}"
+        data = tmp_path / f"data{mode}"
+        code.mkdir()
+        data.mkdir()
+        (code / "params.i").write_text(PARAMS.format(dir=str(data)))
+        np.savetxt(code / "polytrope_gen", M.polytrope(300), fmt="%.17e")
+        (data / "master.pixels").write_text("-10.0\n15.0\n")
+        env = dict(os.environ, SPARC_NSTEPS="46", SPARC_PRECISION="64", SPARC_ADJOINT_SOURCE="waveform",
+                   SPARC_PARTIAL_FITS=mode)
+        shutil.copy(os.path.join(ROOT, "tests", "golden", "Spectral"), code / "Instruction_src01_ls00")
+        assert run_sparc(code, "01", "00", env).returncode == 0
+        shutil.copy(os.path.join(ROOT, "tests", "golden", "Adjoint"), code / "Instruction_src01_ls00")
+        assert run_sparc(code, "01", "00", env).returncode == 0
+        fdir, adir = data / "forward_src01_ls00", data / "adjoint_src01"
+        if mode == "1":
+            assert sorted(f for f in os.listdir(fdir) if f.endswith("_000015_partial.fits")) == [
+                "acc_x_000015_partial.fits", "acc_z_000015_partial.fits", "vx_000015_partial.fits",
+                "vz_000015_partial.fits", "xix_000015_partial.fits", "xiz_000015_partial.fits"]
+            assert not (adir / "xix_000015_partial.fits").exists() and (adir / "vx_000015_partial.fits").exists()
+            assert fits.read(str(fdir / "vz_000030_partial.fits")).shape == (300, 1, 128)
+        os.remove(code / "Instruction_src01_ls00")
+        r = run_sparc(code, "01", "00", env)
+        assert r.returncode == 0, r.stderr
+        assert not any(f.endswith("_partial.fits") for f in os.listdir(fdir))
+        outs[mode] = {n: fits.read(str(data / "kernel" / f"{n}_01.fits")) for n in ("kernel_c", "kernel_psi", "hessian")}
+    for n in outs["0"]:
+        assert np.array_equal(outs["0"][n], outs["1"][n]), n
+
+
 def test_forward_writes_the_travel_time_adjoint_source(tmp_path):
     """A forward run with params.0 present measures f-mode travel times (ADJOINT_SOURCE_FILT):
     ttdiff.0, windows.0, adjoint_src02/{source.fits, information}, kernel/misfit_02_00."""
