@@ -253,7 +253,7 @@ def _load_partial_states(d, forward, ws):
         return np.load(npy)
     if not os.path.isdir(d):
         return None
-    times = sorted(int(f[4:10]) for f in os.listdir(d) if f.startswith("vz_") and f.endswith("_partial.fits"))
+    times = sorted(int(f[3:9]) for f in os.listdir(d) if f.startswith("vz_") and f.endswith("_partial.fits"))
     if not times:
         return None
     from .fits_gpu import read_fields
