@@ -453,7 +453,7 @@ def run_uneven(args):
     solves = M.uneven_solves(48, seed=0)
     if args.nsteps:
         solves = [M.Solve(s.nx, min(s.nsteps, args.nsteps), s.vpeak_ms, s.dcc, s.xloc) for s in solves]
-    ub = UnevenBatch(solves, precision=32, device=f"cuda:{local}")
+    ub = UnevenBatch(solves, precision=32, device=f"cuda:{local}", autotune=args.autotune)
     for _ in range(args.warmup):
         ub.run()
     torch.cuda.synchronize()
@@ -559,6 +559,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain reference path")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy report")
     ap.add_argument("--no-gradient", action="store_true", help="skip the gradient post-processing figures")
+    ap.add_argument("--autotune", action="store_true", help="uneven48: time column-pass variants per group first")
     ap.add_argument("--workload", default="batch32", choices=["batch32", "uneven48", "3d4"],
                     help="uneven48: 48 solves of mixed grids, lengths and backgrounds (seed 0)")
     args = ap.parse_args()

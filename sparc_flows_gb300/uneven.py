@@ -2,8 +2,11 @@
 
 Solves sharing (nx, steps) form one batched plan (per-solve stream function and sound-speed
 multiplier, a per-solve background in HBM); the groups run concurrently, each from its own host
-thread on its own CUDA stream, so that small groups fill the GPU together.  Each group's
-column-pass variant is chosen by timing the candidates on that group's own plan (autotune).  The reference runs
+thread on its own CUDA stream, so that small groups fill the GPU together.  autotune=True picks
+each group's column-pass variant by timing the candidates on that group's own plan; it is off by
+default because a plan timed alone is not a plan timed among eight concurrent ones: on the 48-solve
+workload the tuned choice (the 8-column TMA pass for the 256 and 384 grids) ran at 2.27e9
+grid-point steps/s against 2.46e9 for the default pass.  The reference runs
 every solve as its own single-rank ``sparc`` process (data_forward.sh:28).
 """
 from __future__ import annotations
@@ -53,7 +56,7 @@ def autotune_column(run, model, specs, psi, cmul, precision: int, device, nsteps
 
 
 class UnevenBatch:
-    def __init__(self, solves: list, precision: int = 32, device: str = "cuda:0", autotune: bool = True):
+    def __init__(self, solves: list, precision: int = 32, device: str = "cuda:0", autotune: bool = False):
         self.solves, self.dev = solves, torch.device(device)
         model = M.polytrope(300)
         self.groups = group_solves(solves)
