@@ -253,6 +253,42 @@ int sparc3d_get_state(sparc3d_plan_t *plan, void *dst, void *stream);
 int sparc3d_set_state(sparc3d_plan_t *plan, const void *src, void *stream);
 
 /* ---------------------------------------------------------------------------------------------
+ * 2-D sponge solver: option 5, MP_QUIET_SPONGE_2D (physics2d.f90:1099-1137), the velocity-
+ * pressure-density formulation with a sponge layer instead of a PML (USE_PML off), the RK of
+ * STEP and FILTER_VARS_2D on the five fields.  Fields [nz][nbatch][nx]; the state is five of
+ * them: rho, v_x, v_y (zero), v_z, p (initialize.f90:500-504).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct sparc5_plan sparc5_plan_t;
+
+typedef struct {
+    int nx, nz, nbatch, precision;  /* nx in the FFT table; nz >= 11; precision 32 or 64 */
+    int npmlhor;                    /* FILTER_VARS_2D columns [npmlhor, nx-npmlhor+1] (HORIZONTAL_PMLS) */
+    int filter_all_x;               /* 1: filter every column */
+    double deltat, stretchx;        /* as sparc_config_t */
+    double betas[5];
+    int steps_out, k_src, k_obs;    /* record cadence, 0-based e_rad, o_rad */
+} sparc5_config_t;
+
+/* FP64 device profiles [nz]: stretch, rhoinv, rho0, c2rho0, gradp0_z, gradrho0_z, g (no PML
+ * decay), source_dep, sponge (spongez, physics2d.f90:62-69). */
+typedef struct {
+    const double *stretch, *rhoinv, *rho0, *c2rho0, *gradp0_z, *gradrho0_z, *g, *source_dep, *sponge;
+} sparc5_background_t;
+
+int sparc5_plan_create(const sparc5_config_t *cfg, sparc5_plan_t **plan);
+int sparc5_plan_destroy(sparc5_plan_t *plan);
+int sparc5_set_background(sparc5_plan_t *plan, const sparc5_background_t *bg, void *stream);
+/* forcing(x, step) = pattern[b][x] * amp[step] times source_dep(k) on rows |k - k_src| <= 4
+ * (physics2d.f90:1124-1128); pattern device FP64 [nbatch][nx], amp host [namp]. */
+int sparc5_set_source(sparc5_plan_t *plan, const double *pattern, const double *amp, int namp, void *stream);
+int sparc5_reset_state(sparc5_plan_t *plan, int time0, void *stream);
+/* nsteps steps; v_z at k_obs ([nbatch][nx]) appended to seis after each step whose index is a
+ * multiple of steps_out. */
+int sparc5_forward(sparc5_plan_t *plan, int nsteps, void *seis, int nrec_cap, int *nrec, void *stream);
+/* [5][nz][nbatch][nx] of the plan precision (device). */
+int sparc5_get_state(sparc5_plan_t *plan, void *dst, void *stream);
+
+/* ---------------------------------------------------------------------------------------------
  * Travel-time adjoint source (ADJOINT_SOURCE_FILT, driver.f90:1758-2238), FP64, for a batch of
  * sources.  Records are [nbatch][nt][nx] (x fastest; nt records of vz at o_rad), device.
  * ------------------------------------------------------------------------------------------- */

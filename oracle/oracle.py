@@ -37,7 +37,7 @@ def build(force=False):
     """Compile the oracle with its Makefile (gcc)."""
     if force or not os.path.exists(LIB_PATH) or any(
         os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, f))
-        for f in ("sparc_oracle.c", "sparc_oracle3d.c", "Makefile")
+        for f in ("sparc_oracle.c", "sparc_oracle3d.c", "sparc_oracle_sponge.c", "Makefile")
     ):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH

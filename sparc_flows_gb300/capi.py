@@ -50,6 +50,13 @@ SIGNATURES = {
     "sparc3d_forward": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, _ip, _vp]),
     "sparc3d_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc3d_set_state": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc5_plan_create": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "sparc5_plan_destroy": (ctypes.c_int, [_vp]),
+    "sparc5_set_background": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc5_set_source": (ctypes.c_int, [_vp, _vp, _dp, ctypes.c_int, _vp]),
+    "sparc5_reset_state": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
+    "sparc5_forward": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, _ip, _vp]),
+    "sparc5_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_tt_plan_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             ctypes.POINTER(_vp)]),
     "sparc_tt_plan_destroy": (ctypes.c_int, [_vp]),
@@ -79,6 +86,22 @@ class Sparc3DConfig(ctypes.Structure):
                 ("deltat", ctypes.c_double), ("stretchx", ctypes.c_double), ("stretchy", ctypes.c_double),
                 ("betas", ctypes.c_double * 5), ("flows", ctypes.c_int), ("steps_out", ctypes.c_int),
                 ("k_src", ctypes.c_int), ("k_obs", ctypes.c_int), ("filter_every", ctypes.c_int)]
+
+
+class Sparc5Config(ctypes.Structure):
+    """sparc5_config_t."""
+
+    _fields_ = [("nx", ctypes.c_int), ("nz", ctypes.c_int), ("nbatch", ctypes.c_int), ("precision", ctypes.c_int),
+                ("npmlhor", ctypes.c_int), ("filter_all_x", ctypes.c_int), ("deltat", ctypes.c_double),
+                ("stretchx", ctypes.c_double), ("betas", ctypes.c_double * 5), ("steps_out", ctypes.c_int),
+                ("k_src", ctypes.c_int), ("k_obs", ctypes.c_int)]
+
+
+class Sparc5Background(ctypes.Structure):
+    """sparc5_background_t (device pointers)."""
+
+    _fields_ = [(n, _vp) for n in ("stretch", "rhoinv", "rho0", "c2rho0", "gradp0_z", "gradrho0_z", "g",
+                                    "source_dep", "sponge")]
 
 
 class Sparc3DBackground(ctypes.Structure):

@@ -1647,3 +1647,231 @@ int sparc3d_set_state(sparc3d_plan_t *p, const void *src, void *stream)
 }
 
 }  // extern "C"
+
+// =============================================================================================
+// 2-D sponge plans (option 5): buffers, one time step as a launch sequence, the C ABI.
+// =============================================================================================
+namespace {
+
+template <typename T>
+struct Plan5 {
+    std::vector<void *> allocs;
+    T *A = nullptr, *SCR = nullptr, *X = nullptr, *DVX = nullptr, *DVZ = nullptr, *GX = nullptr, *GZ = nullptr;
+    T *prof = nullptr, *pat = nullptr;
+    DevZ<T> z1;
+    DevFFT<T> fx;
+    S5Bg<T> bg{};
+    const T *stretch = nullptr;
+};
+
+}  // namespace
+
+struct sparc5_plan {
+    sparc5_config_t cfg{};
+    int nch = 0, L = 0;
+    HostZTab hz1;
+    Plan5<float> s32;
+    Plan5<double> s64;
+    std::vector<double> amp;
+    int time = 0;
+    bool have_bg = false;
+    long long F = 0;
+};
+
+namespace {
+
+template <typename T>
+Plan5<T> &plan5(sparc5_plan *p);
+template <>
+Plan5<float> &plan5<float>(sparc5_plan *p) { return p->s32; }
+template <>
+Plan5<double> &plan5<double>(sparc5_plan *p) { return p->s64; }
+
+template <typename T>
+int alloc_plan5(sparc5_plan *p)
+{
+    Plan5<T> &S = plan5<T>(p);
+    const sparc5_config_t &c = p->cfg;
+    const size_t F = (size_t)p->F, nz = c.nz;
+    struct Req { T **ptr; size_t n; };
+    std::vector<Req> reqs = {{&S.A, 5 * F}, {&S.SCR, 5 * F}, {&S.X, 5 * F}, {&S.DVX, F}, {&S.DVZ, F}, {&S.GX, F},
+                             {&S.GZ, F}, {&S.prof, 9 * nz}, {&S.pat, (size_t)c.nbatch * c.nx}};
+    for (auto &r : reqs) {
+        void *ptr = nullptr;
+        const size_t bytes = std::max<size_t>(r.n, 1) * sizeof(T);
+        cudaError_t e = cudaMalloc(&ptr, bytes);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        S.allocs.push_back(ptr);
+        e = cudaMemset(ptr, 0, bytes);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("cudaMemset: ") + cudaGetErrorString(e));
+        *r.ptr = (T *)ptr;
+    }
+    cudaError_t e = upload_ztab<T>(p->hz1, S.z1, S.allocs);
+    if (e == cudaSuccess) e = upload_fft<T>(c.nx, S.fx, S.allocs);
+    if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("tables: ") + cudaGetErrorString(e));
+    T *q = S.prof;
+    S.stretch = q; q += nz;
+    S.bg.rhoinv = q; q += nz;
+    S.bg.rho0 = q; q += nz;
+    S.bg.c2rho0 = q; q += nz;
+    S.bg.gradp0_z = q; q += nz;
+    S.bg.gradrho0_z = q; q += nz;
+    S.bg.g = q; q += nz;
+    S.bg.source_dep = q; q += nz;
+    S.bg.sponge = q;
+    return SPARC_OK;
+}
+
+// STEP for option 5 (step.f90:43-119, physics2d.f90:1099-1137, FILTER_VARS_2D) and the record.
+template <typename T>
+cudaError_t step5(sparc5_plan *p, T *seis, int cap, int &nrec, cudaStream_t st)
+{
+    Plan5<T> &S = plan5<T>(p);
+    const sparc5_config_t &c = p->cfg;
+    const long long F = p->F, lvl = (long long)c.nbatch * c.nx;
+    const S5Args a{c.nx, c.nz, c.nbatch, c.k_src, c.filter_all_x ? 0 : c.npmlhor - 1,
+                   c.filter_all_x ? c.nx - 1 : c.nx - c.npmlhor};
+    const T amp = (T)(p->time >= 0 && p->time < (int)p->amp.size() ? p->amp[p->time] : 0.0);
+    cudaError_t e;
+    for (int s = 0; s < 5; s++) {
+        const T *X = S.A;
+        if (s > 0) {
+            e = launch_s3_stage_in<T>(5 * F, S.A, S.SCR, S.X, (T)c.betas[s], 0, nullptr, nullptr, nullptr, st);
+            if (e != cudaSuccess) return e;
+            X = S.X;
+        }
+        const int nrows = c.nz * c.nbatch;
+        e = launch_ddx<T>(X + F, S.DVX, nrows, c.nx, (T)c.stretchx, S.fx.twr, S.fx.twi, S.fx.kap, st);
+        if (e == cudaSuccess) e = launch_ddx<T>(X + 4 * F, S.GX, nrows, c.nx, (T)c.stretchx, S.fx.twr, S.fx.twi, S.fx.kap, st);
+        if (e == cudaSuccess) e = launch_ddz<T>(S.z1.tab, p->nch, p->L, X + 3 * F, S.DVZ, (int)lvl, c.nz, nullptr, S.stretch, 0, st);
+        if (e == cudaSuccess) e = launch_ddz<T>(S.z1.tab, p->nch, p->L, X + 4 * F, S.GZ, (int)lvl, c.nz, nullptr, S.stretch, 0, st);
+        if (e == cudaSuccess) e = launch_s5_rhs<T>(a, S.bg, X, S.SCR, S.DVX, S.DVZ, S.GX, S.GZ, S.pat, amp, st);
+        if (e != cudaSuccess) return e;
+    }
+    e = launch_s5_end<T>(a, S.A, S.SCR, (T)c.deltat, st);
+    if (e != cudaSuccess) return e;
+    if (c.steps_out > 0 && p->time % c.steps_out == 0) {
+        if (seis && nrec < cap) {
+            e = cudaMemcpyAsync(seis + (size_t)nrec * lvl, S.A + 3 * F + (size_t)c.k_obs * lvl, lvl * sizeof(T),
+                                cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+        nrec++;
+    }
+    p->time++;
+    return cudaSuccess;
+}
+
+template <typename T>
+int set_bg5(sparc5_plan *p, const sparc5_background_t *bg, cudaStream_t st)
+{
+    Plan5<T> &S = plan5<T>(p);
+    const int nz = p->cfg.nz;
+    const double *prof[9] = {bg->stretch, bg->rhoinv, bg->rho0, bg->c2rho0, bg->gradp0_z, bg->gradrho0_z, bg->g,
+                             bg->source_dep, bg->sponge};
+    for (int i = 0; i < 9; i++) CK(cast_to<T>(prof[i], S.prof + (size_t)i * nz, nz, st));
+    return SPARC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sparc5_plan_create(const sparc5_config_t *cfg, sparc5_plan_t **out)
+{
+    if (!cfg || !out) return fail(SPARC_ERR_ARG, "sparc5_plan_create: null argument");
+    *out = nullptr;
+    if (cfg->precision != 32 && cfg->precision != 64) return fail(SPARC_ERR_SIZE, "sparc5_plan_create: precision");
+    if (!fft_size_supported(cfg->nx)) return fail(SPARC_ERR_SIZE, "sparc5_plan_create: nx not in the FFT table");
+    if (cfg->nz < 11 || cfg->nbatch < 1 || cfg->k_src < 0 || cfg->k_src >= cfg->nz || cfg->k_obs < 0 ||
+        cfg->k_obs >= cfg->nz || (!cfg->filter_all_x && (cfg->npmlhor < 1 || 2 * cfg->npmlhor > cfg->nx)) ||
+        (long long)cfg->nz * cfg->nbatch > 2147483647LL)
+        return fail(SPARC_ERR_SIZE, "sparc5_plan_create: bad grid, batch or rows");
+    sparc5_plan *p = new sparc5_plan();
+    p->cfg = *cfg;
+    p->F = (long long)cfg->nx * cfg->nbatch * cfg->nz;
+    if (!chunking(cfg->nz, 16, p->nch, p->L) || !build_ztab(cfg->nz, 1, p->nch, p->L, p->hz1)) {
+        delete p;
+        return fail(SPARC_ERR_SIZE, "sparc5_plan_create: nz too large for the column chunking");
+    }
+    const int rc = cfg->precision == 32 ? alloc_plan5<float>(p) : alloc_plan5<double>(p);
+    if (rc != SPARC_OK) {
+        std::string m = g_err;
+        sparc5_plan_destroy(p);
+        return fail(rc, m);
+    }
+    *out = p;
+    return SPARC_OK;
+}
+
+int sparc5_plan_destroy(sparc5_plan_t *p)
+{
+    if (!p) return SPARC_OK;
+    for (void *q : p->s32.allocs) cudaFree(q);
+    for (void *q : p->s64.allocs) cudaFree(q);
+    delete p;
+    return SPARC_OK;
+}
+
+int sparc5_set_background(sparc5_plan_t *p, const sparc5_background_t *bg, void *stream)
+{
+    if (!p || !bg) return fail(SPARC_ERR_ARG, "sparc5_set_background: null argument");
+    const double *need[9] = {bg->stretch, bg->rhoinv, bg->rho0, bg->c2rho0, bg->gradp0_z, bg->gradrho0_z, bg->g,
+                             bg->source_dep, bg->sponge};
+    for (const double *q : need)
+        if (!q) return fail(SPARC_ERR_ARG, "sparc5_set_background: missing profile");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int rc = p->cfg.precision == 32 ? set_bg5<float>(p, bg, st) : set_bg5<double>(p, bg, st);
+    if (rc == SPARC_OK) p->have_bg = true;
+    return rc;
+}
+
+int sparc5_set_source(sparc5_plan_t *p, const double *pattern, const double *amp, int namp, void *stream)
+{
+    if (!p || !pattern || namp < 0 || (namp > 0 && !amp)) return fail(SPARC_ERR_ARG, "sparc5_set_source: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t n = (size_t)p->cfg.nbatch * p->cfg.nx;
+    if (p->cfg.precision == 32) CK(cast_to<float>(pattern, p->s32.pat, n, st));
+    else CK(cast_to<double>(pattern, p->s64.pat, n, st));
+    p->amp.assign(amp, amp + namp);
+    return SPARC_OK;
+}
+
+int sparc5_reset_state(sparc5_plan_t *p, int time0, void *stream)
+{
+    if (!p) return fail(SPARC_ERR_ARG, "sparc5_reset_state: null plan");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
+    void *A = p->cfg.precision == 32 ? (void *)p->s32.A : (void *)p->s64.A;
+    void *SCR = p->cfg.precision == 32 ? (void *)p->s32.SCR : (void *)p->s64.SCR;
+    CK(cudaMemsetAsync(A, 0, 5 * p->F * es, st));
+    CK(cudaMemsetAsync(SCR, 0, 5 * p->F * es, st));
+    p->time = time0;
+    return SPARC_OK;
+}
+
+int sparc5_forward(sparc5_plan_t *p, int nsteps, void *seis, int nrec_cap, int *nrec, void *stream)
+{
+    if (!p || nsteps < 0 || nrec_cap < 0) return fail(SPARC_ERR_ARG, "sparc5_forward: bad argument");
+    if (!p->have_bg) return fail(SPARC_ERR_STATE, "sparc5_forward: background not set");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int n = 0;
+    for (int i = 0; i < nsteps; i++) {
+        cudaError_t e = p->cfg.precision == 32 ? step5<float>(p, (float *)seis, nrec_cap, n, st)
+                                               : step5<double>(p, (double *)seis, nrec_cap, n, st);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("sparc5_forward: ") + cudaGetErrorString(e));
+    }
+    if (nrec) *nrec = n;
+    return SPARC_OK;
+}
+
+int sparc5_get_state(sparc5_plan_t *p, void *dst, void *stream)
+{
+    if (!p || !dst) return fail(SPARC_ERR_ARG, "sparc5_get_state: null argument");
+    const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
+    const void *A = p->cfg.precision == 32 ? (const void *)p->s32.A : (const void *)p->s64.A;
+    CK(cudaMemcpyAsync(dst, A, 5 * p->F * es, cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
+    return SPARC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,115 @@
+// sparc_sponge.cu -- kernels of the 2-D sponge step (option 5, MP_QUIET_SPONGE_2D,
+// physics2d.f90:1099-1137): the velocity-pressure-density formulation with a sponge layer.
+//
+// Fields are [nz][nb][nx] (level-major, the batch inside a level, as the 3-D step), the state
+// five of them: rho, v_x, v_y (zero in 2-D), v_z, p (initialize.f90:500-504).  One RK stage:
+// X = A + beta SCR (s3_stage_in), x passes of v_x and p (the spectral row pass), z passes of
+// v_z and p (the compact column solve, ibc 1), then s5_rhs_kernel: continuity, momentum with
+// pressure gradient, buoyancy, sponge and source, pressure; the top and bottom rows of the
+// momentum and pressure RHS zero.  End of step: s5_end_kernel, a += dt scr and FILTER_VARS_2D
+// (physics2d.f90:509-560) down each column from a register window, in place.
+#include "sparc_common.cuh"
+
+namespace sparc {
+
+constexpr int S5_THREADS = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(S5_THREADS) s5_rhs_kernel(S5Args a, S5Bg<T> bg, const T *__restrict__ X,
+                                                            T *__restrict__ SCR, const T *__restrict__ DVX,
+                                                            const T *__restrict__ DVZ, const T *__restrict__ GX,
+                                                            const T *__restrict__ GZ, const T *__restrict__ PAT, T amp)
+{
+    const long long lvl = (long long)a.nb * a.nx, n = lvl * a.nz, F = n;
+    const long long stride = (long long)gridDim.x * S5_THREADS;
+    for (long long i = (long long)blockIdx.x * S5_THREADS + threadIdx.x; i < n; i += stride) {
+        const int k = (int)(i / lvl);
+        const long long r = i - (long long)k * lvl;
+        const T rho = X[i], vx = X[F + i], vz = X[3 * F + i], p = X[4 * F + i];
+        const T sp = bg.sponge[k], ri = bg.rhoinv[k];
+        const T div = DVX[i] + DVZ[i];
+        SCR[i] = -bg.gradrho0_z[k] * vz - bg.rho0[k] * div - sp * rho;
+        T rx = -ri * GX[i] - sp * vx;
+        T rz = -ri * GZ[i] - sp * vz;
+        rz = rz - rho * bg.g[k] * ri;
+        if (abs(k - a.e_rad) <= 4) rz = rz + (PAT[r] * amp) * bg.source_dep[k];
+        T rp = -bg.c2rho0[k] * div - vz * bg.gradp0_z[k] - sp * p;
+        if (k == 0 || k == a.nz - 1) rx = rz = rp = T(0);
+        SCR[F + i] = rx;
+        SCR[2 * F + i] = T(0);
+        SCR[3 * F + i] = rz;
+        SCR[4 * F + i] = rp;
+    }
+}
+
+// One thread per (field, column): a += dt scr, then FILTER_VARS_2D: the 11-point filter on rows
+// 5 .. nz-6 and two-point means on rows nz-5 .. nz-2 (0-based) of the updated column, written
+// to rows 5 .. nz-2 for x in [i0, i1] (HORIZONTAL_PMLS) from an 11-value register window.
+template <typename T>
+__global__ void __launch_bounds__(S5_THREADS) s5_end_kernel(S5Args a, T *__restrict__ A, const T *__restrict__ SCR,
+                                                            T dt)
+{
+    const long long lvl = (long long)a.nb * a.nx;
+    const long long cols = 5 * lvl, F = lvl * a.nz;
+    const long long c = (long long)blockIdx.x * S5_THREADS + threadIdx.x;
+    if (c >= cols) return;
+    const int v = (int)(c / lvl);
+    const long long r = c - (long long)v * lvl;
+    const int x = (int)(r % a.nx);
+    T *col = A + (long long)v * F + r;
+    const T *sc = SCR + (long long)v * F + r;
+    const int nz = a.nz;
+    for (int k = 0; k < nz; k++) col[(long long)k * lvl] = col[(long long)k * lvl] + dt * sc[(long long)k * lvl];
+    if (x < a.i0 || x > a.i1 || nz < 11) return;
+    const T c0 = T(0.75390625), h1 = T(0.5 * 0.41015625), h2 = T(0.5 * -0.234375), h3 = T(0.5 * 0.087890625),
+            h4 = T(0.5 * -0.01953125), h5 = T(0.5 * 0.001953125);
+    T w[11];  // rows k-5 .. k+5 of the updated column, for the row k being written
+#pragma unroll
+    for (int j = 0; j < 11; j++) w[j] = col[(long long)j * lvl];
+    for (int k = 5; k <= nz - 2; k++) {
+        T out;
+        if (k <= nz - 6)
+            out = c0 * w[5] + h1 * (w[4] + w[6]) + h2 * (w[3] + w[7]) + h3 * (w[2] + w[8]) + h4 * (w[1] + w[9]) +
+                  h5 * (w[0] + w[10]);
+        else
+            out = T(0.5) * (w[6] + w[4]);
+#pragma unroll
+        for (int j = 0; j < 10; j++) w[j] = w[j + 1];
+        if (k + 6 < nz) w[10] = col[(long long)(k + 6) * lvl];
+        col[(long long)k * lvl] = out;
+    }
+}
+
+static unsigned s5_grid(long long n)
+{
+    const long long g = (n + S5_THREADS - 1) / S5_THREADS;
+    return (unsigned)(g < 152LL * 16 ? g : 152LL * 16);
+}
+
+template <typename T>
+cudaError_t launch_s5_rhs(const S5Args &a, const S5Bg<T> &bg, const T *X, T *SCR, const T *DVX, const T *DVZ,
+                          const T *GX, const T *GZ, const T *PAT, T amp, cudaStream_t st)
+{
+    const long long n = (long long)a.nb * a.nx * a.nz;
+    s5_rhs_kernel<T><<<s5_grid(n), S5_THREADS, 0, st>>>(a, bg, X, SCR, DVX, DVZ, GX, GZ, PAT, amp);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_s5_end(const S5Args &a, T *A, const T *SCR, T dt, cudaStream_t st)
+{
+    const long long cols = 5LL * a.nb * a.nx;
+    s5_end_kernel<T><<<(unsigned)((cols + S5_THREADS - 1) / S5_THREADS), S5_THREADS, 0, st>>>(a, A, SCR, dt);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_s5_rhs<float>(const S5Args &, const S5Bg<float> &, const float *, float *, const float *,
+                                          const float *, const float *, const float *, const float *, float,
+                                          cudaStream_t);
+template cudaError_t launch_s5_rhs<double>(const S5Args &, const S5Bg<double> &, const double *, double *,
+                                           const double *, const double *, const double *, const double *,
+                                           const double *, double, cudaStream_t);
+template cudaError_t launch_s5_end<float>(const S5Args &, float *, const float *, float, cudaStream_t);
+template cudaError_t launch_s5_end<double>(const S5Args &, double *, const double *, double, cudaStream_t);
+
+}  // namespace sparc

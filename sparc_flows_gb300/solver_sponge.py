@@ -1,0 +1,104 @@
+"""2-D sponge solver (option 5, MP_QUIET_SPONGE_2D): the Python host of the sparc5_* C ABI
+(csrc/sparc_sponge.cu, csrc/sparc_capi.cu).
+
+The velocity-pressure-density formulation with a sponge absorber (physics2d.f90:1099-1137),
+the alternative to option 17's displacement formulation with PMLs.  Set-up as the reference's
+mp_Initialize_RHS_2d without PMLs (physics2d.f90:23-230): e_rad, o_rad, source_dep, the sponge
+profile spongez (physics2d.f90:62-69; spongexyz = spongez for a periodic box), rhoinv, c2 rho0
+and the background gradients d rho0/dz, d p0/dz.  State (5, nz, nbatch, nx): rho, v_x, v_y,
+v_z, p.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import capi
+from .config import DIMC, DIMRHO, RSUN_CM
+from .solver import _F32, nearest_level, rk_betas
+from .solver3d import _dbyd2_host
+
+
+class WaveSolverSponge:
+    def __init__(self, nx: int, model: np.ndarray, xlength_cm: float, nbatch: int = 1, precision: int = 64,
+                 timestep: float = 2.0, excitdep_cm: float = -150e5, obsheight_cm: float = 200e5, npmlhor: int = 9,
+                 steps_out: int = 15, filter_all_x: bool = False, device="cuda"):
+        self.L = capi.lib()
+        self.nx, self.nz, self.nb = nx, model.shape[0], nbatch
+        self.dtype = torch.float32 if precision == 32 else torch.float64
+        self.dev = torch.device(device)
+        z = model[:, 0].astype(np.float64)
+        c = model[:, 1] / DIMC
+        rho0 = model[:, 2] / DIMRHO
+        p0 = model[:, 3] / (DIMRHO * DIMC * DIMC)
+        g = model[:, 4] * RSUN_CM / (DIMC * DIMC)
+        self.deltat = timestep * DIMC / RSUN_CM
+        betas = rk_betas(self.deltat)
+        self.e_rad = nearest_level(z, 1.0 + excitdep_cm / RSUN_CM)
+        self.o_rad = nearest_level(z, 1.0 + obsheight_cm / RSUN_CM)
+        stretch = 1.0 / _dbyd2_host(z, 1)
+        f = lambda v: float(_F32(v))  # noqa: E731  single-precision literals of physics2d.f90:65-66
+        sponge = (200.0 / (1.0 + np.exp((f(1.002) - z) / f(0.0001)))
+                  + 300.0 / (1.0 + np.exp((z - (z[0] + f(0.005))) / f(0.0005))))
+        dz = z - z[self.e_rad]
+        self.profiles = dict(stretch=stretch, rhoinv=1.0 / rho0, rho0=rho0, c2rho0=c * c * rho0,
+                             gradp0_z=_dbyd2_host(p0, 1) * stretch, gradrho0_z=_dbyd2_host(rho0, 1) * stretch,
+                             g=g, source_dep=np.exp(-1e7 * 4.0 * (dz * dz)), sponge=sponge)
+        cfg = capi.Sparc5Config()
+        cfg.nx, cfg.nz, cfg.nbatch, cfg.precision = nx, self.nz, nbatch, precision
+        cfg.npmlhor, cfg.filter_all_x = npmlhor, int(filter_all_x)
+        cfg.deltat, cfg.stretchx = self.deltat, RSUN_CM / xlength_cm
+        for i in range(5):
+            cfg.betas[i] = betas[i]
+        cfg.steps_out, cfg.k_src, cfg.k_obs = steps_out, self.e_rad, self.o_rad
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        capi.check(self.L.sparc5_plan_create(ctypes.byref(cfg), ctypes.byref(h)), "sparc5_plan_create")
+        self.plan = h
+        self._bg = {k: torch.as_tensor(v, dtype=torch.float64, device=self.dev) for k, v in self.profiles.items()}
+        bg = capi.Sparc5Background()
+        for k, t in self._bg.items():
+            setattr(bg, k, t.data_ptr())
+        capi.check(self.L.sparc5_set_background(self.plan, ctypes.byref(bg), self._stream()), "sparc5_set_background")
+        torch.cuda.current_stream(self.dev).synchronize()
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def set_source(self, pattern, amp):
+        """forcing(x, step) = pattern[b] * amp[step]: pattern (nb, nx), amp (nsteps,)."""
+        pat = torch.as_tensor(np.ascontiguousarray(pattern), dtype=torch.float64, device=self.dev).contiguous()
+        am = np.ascontiguousarray(amp, dtype=np.float64)
+        capi.check(self.L.sparc5_set_source(self.plan, pat.data_ptr(), am.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                            len(am), self._stream()), "sparc5_set_source")
+        torch.cuda.current_stream(self.dev).synchronize()
+
+    def reset(self, time0: int = 0):
+        capi.check(self.L.sparc5_reset_state(self.plan, time0, self._stream()), "sparc5_reset_state")
+
+    def forward(self, nsteps: int) -> torch.Tensor:
+        """nsteps steps; v_z records (nrec, nb, nx) of the call."""
+        cap = nsteps // max(self.cfg.steps_out, 1) + 1
+        seis = torch.zeros((cap, self.nb, self.nx), dtype=self.dtype, device=self.dev)
+        n = ctypes.c_int(0)
+        capi.check(self.L.sparc5_forward(self.plan, nsteps, seis.data_ptr(), cap, ctypes.byref(n), self._stream()),
+                   "sparc5_forward")
+        return seis[:n.value]
+
+    def state(self) -> torch.Tensor:
+        st = torch.empty((5, self.nz, self.nb, self.nx), dtype=self.dtype, device=self.dev)
+        capi.check(self.L.sparc5_get_state(self.plan, st.data_ptr(), self._stream()), "sparc5_get_state")
+        return st
+
+    def close(self):
+        if getattr(self, "plan", None):
+            self.L.sparc5_plan_destroy(self.plan)
+            self.plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
