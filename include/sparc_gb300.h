@@ -253,9 +253,9 @@ int sparc3d_get_state(sparc3d_plan_t *plan, void *dst, void *stream);
 int sparc3d_set_state(sparc3d_plan_t *plan, const void *src, void *stream);
 
 /* ---------------------------------------------------------------------------------------------
- * 2-D sponge solver: option 5, MP_QUIET_SPONGE_2D (physics2d.f90:1099-1137), the velocity-
- * pressure-density formulation with a sponge layer instead of a PML (USE_PML off), the RK of
- * STEP and FILTER_VARS_2D on the five fields.  Fields [nz][nbatch][nx]; the state is five of
+ * 2-D velocity-pressure-density solver: option 5, MP_QUIET_SPONGE_2D (physics2d.f90:1099-1137,
+ * a sponge layer, USE_PML off) or option 6, MP_QUIET_PML_2D (physics2d.f90:662-713, the
+ * vertical PML), the RK of STEP and FILTER_VARS_2D on the five fields.  Fields [nz][nbatch][nx]; the state is five of
  * them: rho, v_x, v_y (zero), v_z, p (initialize.f90:500-504).
  * ------------------------------------------------------------------------------------------- */
 typedef struct sparc5_plan sparc5_plan_t;
@@ -267,12 +267,16 @@ typedef struct {
     double deltat, stretchx;        /* as sparc_config_t */
     double betas[5];
     int steps_out, k_src, k_obs;    /* record cadence, 0-based e_rad, o_rad */
+    int option;                     /* 5: MP_QUIET_SPONGE_2D (physics2d.f90:1099-1137);
+                                       6: MP_QUIET_PML_2D (physics2d.f90:662-713) */
+    int npmlbot, npmltop;           /* vertical PML levels (option 6) */
 } sparc5_config_t;
 
 /* FP64 device profiles [nz]: stretch, rhoinv, rho0, c2rho0, gradp0_z, gradrho0_z, g (no PML
  * decay), source_dep, sponge (spongez, physics2d.f90:62-69). */
 typedef struct {
     const double *stretch, *rhoinv, *rho0, *c2rho0, *gradp0_z, *gradrho0_z, *g, *source_dep, *sponge;
+    const double *az, *bz;  /* [npmlbot + npmltop] (physics2d.f90:288-332), option 6 */
 } sparc5_background_t;
 
 int sparc5_plan_create(const sparc5_config_t *cfg, sparc5_plan_t **plan);

@@ -12,7 +12,8 @@ _dp = ctypes.POINTER(ctypes.c_double)
 class Orc5Params(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("nz", ctypes.c_int), ("npmlhor", ctypes.c_int),
                 ("xlength", ctypes.c_double), ("timestep", ctypes.c_double), ("excitdep", ctypes.c_double),
-                ("obsheight", ctypes.c_double), ("steps_out", ctypes.c_int), ("filter_all_x", ctypes.c_int)]
+                ("obsheight", ctypes.c_double), ("steps_out", ctypes.c_int), ("filter_all_x", ctypes.c_int),
+                ("option", ctypes.c_int), ("npmlbot", ctypes.c_int), ("npmltop", ctypes.c_int)]
 
 
 _bound = False
@@ -41,14 +42,15 @@ def _p(a):
 
 
 class SimSponge:
-    """One 2-D option-5 solve on the CPU; state (5, nz, nx): rho, v_x, v_y, v_z, p."""
+    """One 2-D option-5 (sponge) or option-6 (PML) solve on the CPU; state (5, nz, nx): rho,
+    v_x, v_y, v_z, p."""
 
     def __init__(self, nx, model, xlength_cm, timestep=2.0, excitdep_cm=-150e5, obsheight_cm=200e5, npmlhor=9,
-                 steps_out=15, filter_all_x=False):
+                 steps_out=15, filter_all_x=False, option=5, npmlbot=10, npmltop=10):
         self.L = _lib()
         self.nx, self.nz = nx, model.shape[0]
         p = Orc5Params(nx, self.nz, npmlhor, xlength_cm, timestep, excitdep_cm, obsheight_cm, steps_out,
-                       int(filter_all_x))
+                       int(filter_all_x), option, npmlbot, npmltop)
         m = np.ascontiguousarray(model, dtype=np.float64)
         self.h = self.L.orc5_create(ctypes.byref(p), _p(m))
         if not self.h:

@@ -1,8 +1,9 @@
 /* sparc_oracle_sponge.c -- CPU FP64 oracle of the 2-D sponge step (test infrastructure).
  *
  * A plain-C restatement of the reference's option 5, MP_QUIET_SPONGE_2D: the velocity-pressure-
- * density formulation with a sponge layer instead of a PML, used only by the tests as the
- * checker of the GPU path (csrc/sparc_sponge.cu).  Fields are [nz][nx], x fastest; the state is
+ * density formulation with a sponge layer instead of a PML, and of option 6, MP_QUIET_PML_2D
+ * (the same formulation with the vertical PML, physics2d.f90:662-713, 1142-1160, 288-332), used
+ * only by the tests as the checker of the GPU path (csrc/sparc_sponge.cu).  Fields are [nz][nx], x fastest; the state is
  * five of them: rho, v_x, v_y (zero in 2-D), v_z, p (initialize.f90:500-512).
  *
  * Followed lines:
@@ -39,6 +40,8 @@ typedef struct {
     double xlength, timestep, excitdep, obsheight;
     int steps_out;
     int filter_all_x; /* 1: every column (HORIZONTAL_PMLS off) */
+    int option;       /* 5: MP_QUIET_SPONGE_2D; 6: MP_QUIET_PML_2D (USE_PML, no sponge) */
+    int npmlbot, npmltop;
 } orc5_params;
 
 typedef struct {
@@ -53,6 +56,9 @@ typedef struct {
     double *fre, *fim, *ftr, *fti;
     double *pattern, *amp;
     int namp, time;
+    int nzpml;
+    double *az, *bz;                    /* [nz], option 6 */
+    double *pmlvars, *psipml, *scrpml;  /* [2][nzpml][nx]: psi_p, psi_vz */
 } orc5_sim;
 
 static double *z5(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
@@ -150,7 +156,90 @@ orc5_sim *orc5_create(const orc5_params *prm, const double *model)
         s->gradrho0_z[k] *= s->stretch[k];
         s->gradp0_z[k] *= s->stretch[k];
     }
+    s->nzpml = prm->option == 6 ? prm->npmlbot + prm->npmltop : 0;
+    s->az = z5(nz); s->bz = z5(nz);
+    s->pmlvars = z5(2 * (size_t)s->nzpml * nx); s->psipml = z5(2 * (size_t)s->nzpml * nx);
+    s->scrpml = z5(2 * (size_t)s->nzpml * nx);
+    if (prm->option == 6) {
+        /* USE_PML: no sponge (physics2d.f90:289-290) and the vertical PML of physics2d.f90:288-332
+         * (laterally uniform background; the top layer's damping takes c at level nz-5) */
+        const int nb = prm->npmlbot, nt = prm->npmltop;
+        const double l005 = (double)0.005f;
+        const double *z = s->z;
+        for (int k = 0; k < nz; k++) {
+            s->sponge[k] = 0.0;
+            double alk = ORC5_PI * l005 * diml / dimc, dampz = 0.0;
+            if (k < nb) {
+                alk = ORC5_PI * l005 * diml / dimc * (z[k] - z[0]) / (z[nb - 1] - z[0]);
+                const double rr = (z[nb - 1] - z[k]) / (z[nb - 1] - z[0]);
+                dampz = 3. * 3. * sqrt(s->c2[0]) / (z[nb - 1] - z[0]) * (rr * rr);
+                const double fd = alk / (dampz + alk);
+                s->gradp0_z[k] *= fd;
+                s->gradrho0_z[k] *= fd;
+                s->g[k] *= fd;
+            }
+            if (k > nz - nt - 1) {
+                alk = ORC5_PI * l005 * diml / dimc * (z[nz - 1] - z[k]) / (z[nz - 1] - z[nz - nt]);
+                const double rr = (z[nz - nt] - z[k]) / (z[nz - 1] - z[nz - nt]);
+                dampz = 3. * 3. * sqrt(s->c2[nz - 6]) / (z[nz - 1] - z[nz - nt]) * (rr * rr);
+                const double fd = alk / (dampz + alk);
+                s->gradp0_z[k] *= fd;
+                s->gradrho0_z[k] *= fd;
+                s->g[k] *= fd;
+            }
+            s->bz[k] = -alk - dampz;
+            s->az[k] = -dampz;
+        }
+    }
     return s;
+}
+
+static int pml5(const orc5_sim *s, int k)
+{
+    if (k < s->p.npmlbot) return k;
+    if (k >= s->nz - s->p.npmltop) return s->p.npmlbot + (k - (s->nz - s->p.npmltop));
+    return -1;
+}
+
+/* MP_QUIET_PML_2D (physics2d.f90:662-713) with PML_BOUNDARY_ACCOUNTING_2D (1142-1160). */
+static void orc6_rhs(orc5_sim *s)
+{
+    const int nx = s->nx, nz = s->nz;
+    const size_t N = s->N, P = (size_t)s->nzpml * nx;
+    const double *rho = s->temp, *vx = s->temp + N, *vz = s->temp + 3 * N, *p = s->temp + 4 * N;
+    double *rc = s->scr, *rvx = s->scr + N, *rvy = s->scr + 2 * N, *rvz = s->scr + 3 * N, *rp = s->scr + 4 * N;
+    d5_z(s, vz, s->dvzdz, 1);
+    d5_z(s, p, s->gpz, 1);
+    for (int k = 0; k < nz; k++) {
+        const int pi = pml5(s, k);
+        if (pi < 0) continue;
+        for (int i = 0; i < nx; i++) {
+            const size_t q = (size_t)k * nx + i, m = (size_t)pi * nx + i;
+            s->scrpml[m] = s->az[k] * s->gpz[q] + s->bz[k] * s->psipml[m];
+            s->gpz[q] = s->gpz[q] + s->psipml[m];
+            s->scrpml[P + m] = s->az[k] * s->dvzdz[q] + s->bz[k] * s->psipml[P + m];
+            s->dvzdz[q] = s->dvzdz[q] + s->psipml[P + m];
+        }
+    }
+    d5_x(s, vx, s->dvxdx);
+    d5_x(s, p, s->gpx);
+    const double amp = s->time < s->namp ? s->amp[s->time] : 0.0;
+    for (int k = 0; k < nz; k++)
+        for (int i = 0; i < nx; i++) {
+            const size_t q = (size_t)k * nx + i;
+            const double div = s->dvxdx[q] + s->dvzdz[q];
+            rc[q] = -s->rho0[k] * div - s->gradrho0_z[k] * vz[q];
+            rp[q] = -s->c2rho0[k] * div - vz[q] * s->gradp0_z[k];
+            rvx[q] = -s->rhoinv[k] * s->gpx[q];
+            double r = -s->rhoinv[k] * (s->gpz[q] + rho[q] * s->g[k]);
+            if (abs(k - s->e_rad) <= 4) r = r + (s->pattern[i] * amp) * s->source_dep[k];
+            rvz[q] = r;
+            rvy[q] = 0.0;
+        }
+    for (int i = 0; i < nx; i++) {
+        const size_t t0 = i, t1 = (size_t)(nz - 1) * nx + i;
+        rvx[t0] = rvx[t1] = rvz[t0] = rvz[t1] = rp[t0] = rp[t1] = rc[t0] = rc[t1] = 0.0;
+    }
 }
 
 void orc5_destroy(orc5_sim *s)
@@ -158,7 +247,8 @@ void orc5_destroy(orc5_sim *s)
     if (!s) return;
     double *ptrs[] = {s->fre, s->fim, s->ftr, s->fti, s->z, s->stretch, s->g, s->rho0, s->p0, s->c2, s->rhoinv,
                       s->c2rho0, s->gradrho0_z, s->gradp0_z, s->sponge, s->source_dep, s->a, s->temp, s->scr,
-                      s->dvxdx, s->dvzdz, s->gpx, s->gpz, s->tmp, s->pattern, s->amp};
+                      s->dvxdx, s->dvzdz, s->gpx, s->gpz, s->tmp, s->pattern, s->amp, s->az, s->bz,
+                      s->pmlvars, s->psipml, s->scrpml};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
     orc_fft_delete(s->fx);
     free(s);
@@ -235,14 +325,20 @@ static void orc5_filter(orc5_sim *s)
 
 void orc5_step(orc5_sim *s)
 {
-    const size_t N5 = 5 * s->N;
+    const size_t N5 = 5 * s->N, P2 = 2 * (size_t)s->nzpml * s->nx;
     for (int rk = 0; rk < 5; rk++) {
-        if (rk == 0) memcpy(s->temp, s->a, N5 * sizeof(double));
-        else
+        if (rk == 0) {
+            memcpy(s->temp, s->a, N5 * sizeof(double));
+            memcpy(s->psipml, s->pmlvars, P2 * sizeof(double));
+        } else {
             for (size_t q = 0; q < N5; q++) s->temp[q] = s->a[q] + s->betas[rk] * s->scr[q];
-        orc5_rhs(s);
+            for (size_t q = 0; q < P2; q++) s->psipml[q] = s->pmlvars[q] + s->betas[rk] * s->scrpml[q];
+        }
+        if (s->p.option == 6) orc6_rhs(s);
+        else orc5_rhs(s);
     }
     for (size_t q = 0; q < N5; q++) s->a[q] = s->a[q] + s->deltat * s->scr[q];
+    for (size_t q = 0; q < P2; q++) s->pmlvars[q] = s->pmlvars[q] + s->deltat * s->scrpml[q];
     orc5_filter(s);
 }
 
@@ -277,6 +373,9 @@ long orc5_get_profile(const orc5_sim *s, const char *name, double *out)
 {
     const double *src = NULL;
     if (!strcmp(name, "sponge")) src = s->sponge;
+    else if (!strcmp(name, "az")) src = s->az;
+    else if (!strcmp(name, "bz")) src = s->bz;
+    else if (!strcmp(name, "g")) src = s->g;
     else if (!strcmp(name, "stretch")) src = s->stretch;
     else if (!strcmp(name, "gradp0_z")) src = s->gradp0_z;
     else if (!strcmp(name, "gradrho0_z")) src = s->gradrho0_z;

@@ -94,14 +94,15 @@ class Sparc5Config(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("nz", ctypes.c_int), ("nbatch", ctypes.c_int), ("precision", ctypes.c_int),
                 ("npmlhor", ctypes.c_int), ("filter_all_x", ctypes.c_int), ("deltat", ctypes.c_double),
                 ("stretchx", ctypes.c_double), ("betas", ctypes.c_double * 5), ("steps_out", ctypes.c_int),
-                ("k_src", ctypes.c_int), ("k_obs", ctypes.c_int)]
+                ("k_src", ctypes.c_int), ("k_obs", ctypes.c_int), ("option", ctypes.c_int),
+                ("npmlbot", ctypes.c_int), ("npmltop", ctypes.c_int)]
 
 
 class Sparc5Background(ctypes.Structure):
     """sparc5_background_t (device pointers)."""
 
     _fields_ = [(n, _vp) for n in ("stretch", "rhoinv", "rho0", "c2rho0", "gradp0_z", "gradrho0_z", "g",
-                                    "source_dep", "sponge")]
+                                    "source_dep", "sponge", "az", "bz")]
 
 
 class Sparc3DBackground(ctypes.Structure):

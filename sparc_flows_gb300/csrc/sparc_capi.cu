@@ -1658,6 +1658,7 @@ struct Plan5 {
     std::vector<void *> allocs;
     T *A = nullptr, *SCR = nullptr, *X = nullptr, *DVX = nullptr, *DVZ = nullptr, *GX = nullptr, *GZ = nullptr;
     T *prof = nullptr, *pat = nullptr;
+    T *PV = nullptr, *SPV = nullptr, *PSI = nullptr;  // option 6: psi_p, psi_vz [2][npml][nb][nx]
     DevZ<T> z1;
     DevFFT<T> fx;
     S5Bg<T> bg{};
@@ -1692,10 +1693,12 @@ int alloc_plan5(sparc5_plan *p)
 {
     Plan5<T> &S = plan5<T>(p);
     const sparc5_config_t &c = p->cfg;
-    const size_t F = (size_t)p->F, nz = c.nz;
+    const size_t F = (size_t)p->F, nz = c.nz, npml = c.option == 6 ? c.npmlbot + c.npmltop : 0;
+    const size_t P2 = 2 * npml * c.nbatch * c.nx;
     struct Req { T **ptr; size_t n; };
     std::vector<Req> reqs = {{&S.A, 5 * F}, {&S.SCR, 5 * F}, {&S.X, 5 * F}, {&S.DVX, F}, {&S.DVZ, F}, {&S.GX, F},
-                             {&S.GZ, F}, {&S.prof, 9 * nz}, {&S.pat, (size_t)c.nbatch * c.nx}};
+                             {&S.GZ, F}, {&S.prof, 9 * nz + 2 * npml}, {&S.pat, (size_t)c.nbatch * c.nx},
+                             {&S.PV, P2}, {&S.SPV, P2}, {&S.PSI, P2}};
     for (auto &r : reqs) {
         void *ptr = nullptr;
         const size_t bytes = std::max<size_t>(r.n, 1) * sizeof(T);
@@ -1718,7 +1721,9 @@ int alloc_plan5(sparc5_plan *p)
     S.bg.gradrho0_z = q; q += nz;
     S.bg.g = q; q += nz;
     S.bg.source_dep = q; q += nz;
-    S.bg.sponge = q;
+    S.bg.sponge = q; q += nz;
+    S.bg.az = q; q += npml;
+    S.bg.bz = q;
     return SPARC_OK;
 }
 
@@ -1729,26 +1734,31 @@ cudaError_t step5(sparc5_plan *p, T *seis, int cap, int &nrec, cudaStream_t st)
     Plan5<T> &S = plan5<T>(p);
     const sparc5_config_t &c = p->cfg;
     const long long F = p->F, lvl = (long long)c.nbatch * c.nx;
+    const bool pml = c.option == 6;
     const S5Args a{c.nx, c.nz, c.nbatch, c.k_src, c.filter_all_x ? 0 : c.npmlhor - 1,
-                   c.filter_all_x ? c.nx - 1 : c.nx - c.npmlhor};
+                   c.filter_all_x ? c.nx - 1 : c.nx - c.npmlhor, pml ? c.npmlbot : 0, pml ? c.npmltop : 0};
+    const long long P2 = pml ? 2LL * (c.npmlbot + c.npmltop) * lvl : 0;
     const T amp = (T)(p->time >= 0 && p->time < (int)p->amp.size() ? p->amp[p->time] : 0.0);
     cudaError_t e;
     for (int s = 0; s < 5; s++) {
-        const T *X = S.A;
+        const T *X = S.A, *PSI = S.PV;
         if (s > 0) {
-            e = launch_s3_stage_in<T>(5 * F, S.A, S.SCR, S.X, (T)c.betas[s], 0, nullptr, nullptr, nullptr, st);
+            e = launch_s3_stage_in<T>(5 * F, S.A, S.SCR, S.X, (T)c.betas[s], P2, S.PV, S.SPV, S.PSI, st);
             if (e != cudaSuccess) return e;
             X = S.X;
+            PSI = S.PSI;
         }
         const int nrows = c.nz * c.nbatch;
         e = launch_ddx<T>(X + F, S.DVX, nrows, c.nx, (T)c.stretchx, S.fx.twr, S.fx.twi, S.fx.kap, st);
         if (e == cudaSuccess) e = launch_ddx<T>(X + 4 * F, S.GX, nrows, c.nx, (T)c.stretchx, S.fx.twr, S.fx.twi, S.fx.kap, st);
         if (e == cudaSuccess) e = launch_ddz<T>(S.z1.tab, p->nch, p->L, X + 3 * F, S.DVZ, (int)lvl, c.nz, nullptr, S.stretch, 0, st);
         if (e == cudaSuccess) e = launch_ddz<T>(S.z1.tab, p->nch, p->L, X + 4 * F, S.GZ, (int)lvl, c.nz, nullptr, S.stretch, 0, st);
-        if (e == cudaSuccess) e = launch_s5_rhs<T>(a, S.bg, X, S.SCR, S.DVX, S.DVZ, S.GX, S.GZ, S.pat, amp, st);
+        if (e == cudaSuccess)
+            e = pml ? launch_s6_rhs<T>(a, S.bg, X, S.SCR, S.DVX, S.DVZ, S.GX, S.GZ, PSI, S.SPV, S.pat, amp, st)
+                    : launch_s5_rhs<T>(a, S.bg, X, S.SCR, S.DVX, S.DVZ, S.GX, S.GZ, S.pat, amp, st);
         if (e != cudaSuccess) return e;
     }
-    e = launch_s5_end<T>(a, S.A, S.SCR, (T)c.deltat, st);
+    e = launch_s5_end<T>(a, S.A, S.SCR, (T)c.deltat, pml ? S.PV : nullptr, S.SPV, st);
     if (e != cudaSuccess) return e;
     if (c.steps_out > 0 && p->time % c.steps_out == 0) {
         if (seis && nrec < cap) {
@@ -1770,6 +1780,11 @@ int set_bg5(sparc5_plan *p, const sparc5_background_t *bg, cudaStream_t st)
     const double *prof[9] = {bg->stretch, bg->rhoinv, bg->rho0, bg->c2rho0, bg->gradp0_z, bg->gradrho0_z, bg->g,
                              bg->source_dep, bg->sponge};
     for (int i = 0; i < 9; i++) CK(cast_to<T>(prof[i], S.prof + (size_t)i * nz, nz, st));
+    if (p->cfg.option == 6) {
+        const int npml = p->cfg.npmlbot + p->cfg.npmltop;
+        CK(cast_to<T>(bg->az, S.prof + (size_t)9 * nz, npml, st));
+        CK(cast_to<T>(bg->bz, S.prof + (size_t)9 * nz + npml, npml, st));
+    }
     return SPARC_OK;
 }
 
@@ -1787,6 +1802,9 @@ int sparc5_plan_create(const sparc5_config_t *cfg, sparc5_plan_t **out)
         cfg->k_obs >= cfg->nz || (!cfg->filter_all_x && (cfg->npmlhor < 1 || 2 * cfg->npmlhor > cfg->nx)) ||
         (long long)cfg->nz * cfg->nbatch > 2147483647LL)
         return fail(SPARC_ERR_SIZE, "sparc5_plan_create: bad grid, batch or rows");
+    if ((cfg->option != 5 && cfg->option != 6) ||
+        (cfg->option == 6 && (cfg->npmlbot < 1 || cfg->npmltop < 1 || cfg->npmlbot + cfg->npmltop >= cfg->nz)))
+        return fail(SPARC_ERR_ARG, "sparc5_plan_create: option must be 5 or 6 (with PML levels for 6)");
     sparc5_plan *p = new sparc5_plan();
     p->cfg = *cfg;
     p->F = (long long)cfg->nx * cfg->nbatch * cfg->nz;
@@ -1820,6 +1838,7 @@ int sparc5_set_background(sparc5_plan_t *p, const sparc5_background_t *bg, void 
                              bg->source_dep, bg->sponge};
     for (const double *q : need)
         if (!q) return fail(SPARC_ERR_ARG, "sparc5_set_background: missing profile");
+    if (p->cfg.option == 6 && (!bg->az || !bg->bz)) return fail(SPARC_ERR_ARG, "sparc5_set_background: PML az, bz missing");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int rc = p->cfg.precision == 32 ? set_bg5<float>(p, bg, st) : set_bg5<double>(p, bg, st);
     if (rc == SPARC_OK) p->have_bg = true;
@@ -1846,6 +1865,13 @@ int sparc5_reset_state(sparc5_plan_t *p, int time0, void *stream)
     void *SCR = p->cfg.precision == 32 ? (void *)p->s32.SCR : (void *)p->s64.SCR;
     CK(cudaMemsetAsync(A, 0, 5 * p->F * es, st));
     CK(cudaMemsetAsync(SCR, 0, 5 * p->F * es, st));
+    if (p->cfg.option == 6) {
+        const size_t P2 = 2 * (size_t)(p->cfg.npmlbot + p->cfg.npmltop) * p->cfg.nbatch * p->cfg.nx;
+        void *PV = p->cfg.precision == 32 ? (void *)p->s32.PV : (void *)p->s64.PV;
+        void *SPV = p->cfg.precision == 32 ? (void *)p->s32.SPV : (void *)p->s64.SPV;
+        CK(cudaMemsetAsync(PV, 0, P2 * es, st));
+        CK(cudaMemsetAsync(SPV, 0, P2 * es, st));
+    }
     p->time = time0;
     return SPARC_OK;
 }

@@ -438,16 +438,20 @@ cudaError_t launch_s3_end(const S3Args &a, T *A, const T *SCR, T dt, int filter,
 // 2-D sponge step (option 5, sparc_sponge.cu).  Fields [nz][nb][nx].
 struct S5Args {
     int nx, nz, nb, e_rad, i0, i1;  // filter columns [i0, i1]
+    int npmlbot, npmltop;           // option 6
 };
 template <typename T>
-struct S5Bg {  // profiles in z
-    const T *rhoinv, *rho0, *c2rho0, *gradp0_z, *gradrho0_z, *g, *source_dep, *sponge;
+struct S5Bg {  // profiles in z; az, bz [npmlbot + npmltop] (option 6)
+    const T *rhoinv, *rho0, *c2rho0, *gradp0_z, *gradrho0_z, *g, *source_dep, *sponge, *az, *bz;
 };
 template <typename T>
 cudaError_t launch_s5_rhs(const S5Args &a, const S5Bg<T> &bg, const T *X, T *SCR, const T *DVX, const T *DVZ,
                           const T *GX, const T *GZ, const T *PAT, T amp, cudaStream_t st);
 template <typename T>
-cudaError_t launch_s5_end(const S5Args &a, T *A, const T *SCR, T dt, cudaStream_t st);
+cudaError_t launch_s6_rhs(const S5Args &a, const S5Bg<T> &bg, const T *X, T *SCR, const T *DVX, const T *DVZ,
+                          const T *GX, const T *GZ, const T *PSI, T *SPSI, const T *PAT, T amp, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s5_end(const S5Args &a, T *A, const T *SCR, T dt, T *PV, const T *SPV, cudaStream_t st);
 
 template <int CW, int R>
 cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st);

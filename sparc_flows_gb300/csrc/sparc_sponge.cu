@@ -1,5 +1,6 @@
-// sparc_sponge.cu -- kernels of the 2-D sponge step (option 5, MP_QUIET_SPONGE_2D,
-// physics2d.f90:1099-1137): the velocity-pressure-density formulation with a sponge layer.
+// sparc_sponge.cu -- kernels of the 2-D velocity-pressure-density steps: option 5
+// (MP_QUIET_SPONGE_2D, physics2d.f90:1099-1137, a sponge layer) and option 6 (MP_QUIET_PML_2D,
+// physics2d.f90:662-713, the vertical PML).
 //
 // Fields are [nz][nb][nx] (level-major, the batch inside a level, as the 3-D step), the state
 // five of them: rho, v_x, v_y (zero in 2-D), v_z, p (initialize.f90:500-504).  One RK stage:
@@ -40,6 +41,59 @@ __global__ void __launch_bounds__(S5_THREADS) s5_rhs_kernel(S5Args a, S5Bg<T> bg
         SCR[3 * F + i] = rz;
         SCR[4 * F + i] = rp;
     }
+}
+
+// Option 6, MP_QUIET_PML_2D (physics2d.f90:662-713): the same formulation with the vertical PML
+// (PML_BOUNDARY_ACCOUNTING_2D, physics2d.f90:1142-1160: psi_p and psi_vz on the PML rows,
+// stored [2][npml][nb][nx]) and no sponge; the top and bottom rows of all four RHS zero.
+template <typename T>
+__global__ void __launch_bounds__(S5_THREADS) s6_rhs_kernel(S5Args a, S5Bg<T> bg, const T *__restrict__ X,
+                                                            T *__restrict__ SCR, const T *__restrict__ DVX,
+                                                            const T *__restrict__ DVZ, const T *__restrict__ GX,
+                                                            const T *__restrict__ GZ, const T *__restrict__ PSI,
+                                                            T *__restrict__ SPSI, const T *__restrict__ PAT, T amp)
+{
+    const long long lvl = (long long)a.nb * a.nx, n = lvl * a.nz, F = n;
+    const long long P = (long long)(a.npmlbot + a.npmltop) * lvl;
+    const long long stride = (long long)gridDim.x * S5_THREADS;
+    for (long long i = (long long)blockIdx.x * S5_THREADS + threadIdx.x; i < n; i += stride) {
+        const int k = (int)(i / lvl);
+        const long long r = i - (long long)k * lvl;
+        T gz = GZ[i], dvz = DVZ[i];
+        int pi = -1;
+        if (k < a.npmlbot) pi = k;
+        else if (k >= a.nz - a.npmltop) pi = a.npmlbot + (k - (a.nz - a.npmltop));
+        if (pi >= 0) {
+            const long long m = (long long)pi * lvl + r;
+            const T pp = PSI[m], pv = PSI[P + m];
+            SPSI[m] = bg.az[pi] * gz + bg.bz[pi] * pp;
+            gz = gz + pp;
+            SPSI[P + m] = bg.az[pi] * dvz + bg.bz[pi] * pv;
+            dvz = dvz + pv;
+        }
+        const T rho = X[i], vz = X[3 * F + i];
+        const T ri = bg.rhoinv[k];
+        const T div = DVX[i] + dvz;
+        T rc = -bg.rho0[k] * div - bg.gradrho0_z[k] * vz;
+        T rp = -bg.c2rho0[k] * div - vz * bg.gradp0_z[k];
+        T rx = -ri * GX[i];
+        T rz = -ri * (gz + rho * bg.g[k]);
+        if (abs(k - a.e_rad) <= 4) rz = rz + (PAT[r] * amp) * bg.source_dep[k];
+        if (k == 0 || k == a.nz - 1) rc = rp = rx = rz = T(0);
+        SCR[i] = rc;
+        SCR[F + i] = rx;
+        SCR[2 * F + i] = T(0);
+        SCR[3 * F + i] = rz;
+        SCR[4 * F + i] = rp;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(S5_THREADS) s5_axpy_kernel(long long n, T *__restrict__ Y, const T *__restrict__ X,
+                                                             T a)
+{
+    const long long stride = (long long)gridDim.x * S5_THREADS;
+    for (long long i = (long long)blockIdx.x * S5_THREADS + threadIdx.x; i < n; i += stride) Y[i] = Y[i] + a * X[i];
 }
 
 // One thread per (field, column): a += dt scr, then FILTER_VARS_2D: the 11-point filter on rows
@@ -96,10 +150,21 @@ cudaError_t launch_s5_rhs(const S5Args &a, const S5Bg<T> &bg, const T *X, T *SCR
 }
 
 template <typename T>
-cudaError_t launch_s5_end(const S5Args &a, T *A, const T *SCR, T dt, cudaStream_t st)
+cudaError_t launch_s6_rhs(const S5Args &a, const S5Bg<T> &bg, const T *X, T *SCR, const T *DVX, const T *DVZ,
+                          const T *GX, const T *GZ, const T *PSI, T *SPSI, const T *PAT, T amp, cudaStream_t st)
+{
+    const long long n = (long long)a.nb * a.nx * a.nz;
+    s6_rhs_kernel<T><<<s5_grid(n), S5_THREADS, 0, st>>>(a, bg, X, SCR, DVX, DVZ, GX, GZ, PSI, SPSI, PAT, amp);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_s5_end(const S5Args &a, T *A, const T *SCR, T dt, T *PV, const T *SPV, cudaStream_t st)
 {
     const long long cols = 5LL * a.nb * a.nx;
     s5_end_kernel<T><<<(unsigned)((cols + S5_THREADS - 1) / S5_THREADS), S5_THREADS, 0, st>>>(a, A, SCR, dt);
+    const long long np = 2LL * (a.npmlbot + a.npmltop) * a.nb * a.nx;
+    if (PV && np > 0) s5_axpy_kernel<T><<<s5_grid(np), S5_THREADS, 0, st>>>(np, PV, SPV, dt);
     return cudaGetLastError();
 }
 
@@ -109,7 +174,15 @@ template cudaError_t launch_s5_rhs<float>(const S5Args &, const S5Bg<float> &, c
 template cudaError_t launch_s5_rhs<double>(const S5Args &, const S5Bg<double> &, const double *, double *,
                                            const double *, const double *, const double *, const double *,
                                            const double *, double, cudaStream_t);
-template cudaError_t launch_s5_end<float>(const S5Args &, float *, const float *, float, cudaStream_t);
-template cudaError_t launch_s5_end<double>(const S5Args &, double *, const double *, double, cudaStream_t);
+template cudaError_t launch_s6_rhs<float>(const S5Args &, const S5Bg<float> &, const float *, float *, const float *,
+                                          const float *, const float *, const float *, const float *, float *,
+                                          const float *, float, cudaStream_t);
+template cudaError_t launch_s6_rhs<double>(const S5Args &, const S5Bg<double> &, const double *, double *,
+                                           const double *, const double *, const double *, const double *,
+                                           const double *, double *, const double *, double, cudaStream_t);
+template cudaError_t launch_s5_end<float>(const S5Args &, float *, const float *, float, float *, const float *,
+                                          cudaStream_t);
+template cudaError_t launch_s5_end<double>(const S5Args &, double *, const double *, double, double *,
+                                           const double *, cudaStream_t);
 
 }  // namespace sparc

@@ -1,11 +1,12 @@
-"""2-D sponge solver (option 5, MP_QUIET_SPONGE_2D): the Python host of the sparc5_* C ABI
-(csrc/sparc_sponge.cu, csrc/sparc_capi.cu).
+"""2-D velocity-pressure-density solver: option 5 (MP_QUIET_SPONGE_2D, a sponge absorber,
+physics2d.f90:1099-1137) or option 6 (MP_QUIET_PML_2D, the vertical PML, physics2d.f90:662-713);
+the Python host of the sparc5_* C ABI (csrc/sparc_sponge.cu, csrc/sparc_capi.cu).
 
-The velocity-pressure-density formulation with a sponge absorber (physics2d.f90:1099-1137),
-the alternative to option 17's displacement formulation with PMLs.  Set-up as the reference's
-mp_Initialize_RHS_2d without PMLs (physics2d.f90:23-230): e_rad, o_rad, source_dep, the sponge
-profile spongez (physics2d.f90:62-69; spongexyz = spongez for a periodic box), rhoinv, c2 rho0
-and the background gradients d rho0/dz, d p0/dz.  State (5, nz, nbatch, nx): rho, v_x, v_y,
+Set-up as the reference's mp_Initialize_RHS_2d (physics2d.f90:23-332): e_rad, o_rad,
+source_dep, rhoinv, c2 rho0, the background gradients d rho0/dz, d p0/dz, and either the sponge
+profile spongez (physics2d.f90:62-69; spongexyz = spongez for a periodic box) or, with USE_PML,
+no sponge (physics2d.f90:289-290) and the vertical PML coefficients with their decay of the
+background gradients and g (physics2d.f90:288-332).  State (5, nz, nbatch, nx): rho, v_x, v_y,
 v_z, p.
 """
 from __future__ import annotations
@@ -17,14 +18,15 @@ import torch
 
 from . import capi
 from .config import DIMC, DIMRHO, RSUN_CM
-from .solver import _F32, nearest_level, rk_betas
+from .solver import PI, _F32, nearest_level, rk_betas
 from .solver3d import _dbyd2_host
 
 
 class WaveSolverSponge:
     def __init__(self, nx: int, model: np.ndarray, xlength_cm: float, nbatch: int = 1, precision: int = 64,
                  timestep: float = 2.0, excitdep_cm: float = -150e5, obsheight_cm: float = 200e5, npmlhor: int = 9,
-                 steps_out: int = 15, filter_all_x: bool = False, device="cuda"):
+                 steps_out: int = 15, filter_all_x: bool = False, option: int = 5, npmlbot: int = 10,
+                 npmltop: int = 10, device="cuda"):
         self.L = capi.lib()
         self.nx, self.nz, self.nb = nx, model.shape[0], nbatch
         self.dtype = torch.float32 if precision == 32 else torch.float64
@@ -43,9 +45,36 @@ class WaveSolverSponge:
         sponge = (200.0 / (1.0 + np.exp((f(1.002) - z) / f(0.0001)))
                   + 300.0 / (1.0 + np.exp((z - (z[0] + f(0.005))) / f(0.0005))))
         dz = z - z[self.e_rad]
+        gp0 = _dbyd2_host(p0, 1) * stretch
+        gr0 = _dbyd2_host(rho0, 1) * stretch
+        nz = self.nz
+        az = np.zeros(npmlbot + npmltop)
+        bz = np.zeros(npmlbot + npmltop)
+        if option == 6:
+            sponge = np.zeros(nz)
+            l005 = f(0.005)
+            for k in range(nz):
+                if k < npmlbot:
+                    alk = PI * l005 * RSUN_CM / DIMC * (z[k] - z[0]) / (z[npmlbot - 1] - z[0])
+                    rr = (z[npmlbot - 1] - z[k]) / (z[npmlbot - 1] - z[0])
+                    dampz = 3.0 * 3.0 * c[0] / (z[npmlbot - 1] - z[0]) * (rr * rr)
+                    pi_ = k
+                elif k > nz - npmltop - 1:
+                    alk = PI * l005 * RSUN_CM / DIMC * (z[nz - 1] - z[k]) / (z[nz - 1] - z[nz - npmltop])
+                    rr = (z[nz - npmltop] - z[k]) / (z[nz - 1] - z[nz - npmltop])
+                    dampz = 3.0 * 3.0 * c[nz - 6] / (z[nz - 1] - z[nz - npmltop]) * (rr * rr)
+                    pi_ = npmlbot + (k - (nz - npmltop))
+                else:
+                    continue
+                fd = alk / (dampz + alk)
+                gp0[k] *= fd
+                gr0[k] *= fd
+                g[k] *= fd
+                az[pi_] = -dampz
+                bz[pi_] = -alk - dampz
         self.profiles = dict(stretch=stretch, rhoinv=1.0 / rho0, rho0=rho0, c2rho0=c * c * rho0,
-                             gradp0_z=_dbyd2_host(p0, 1) * stretch, gradrho0_z=_dbyd2_host(rho0, 1) * stretch,
-                             g=g, source_dep=np.exp(-1e7 * 4.0 * (dz * dz)), sponge=sponge)
+                             gradp0_z=gp0, gradrho0_z=gr0, g=g, source_dep=np.exp(-1e7 * 4.0 * (dz * dz)),
+                             sponge=sponge, az=az, bz=bz)
         cfg = capi.Sparc5Config()
         cfg.nx, cfg.nz, cfg.nbatch, cfg.precision = nx, self.nz, nbatch, precision
         cfg.npmlhor, cfg.filter_all_x = npmlhor, int(filter_all_x)
@@ -53,6 +82,7 @@ class WaveSolverSponge:
         for i in range(5):
             cfg.betas[i] = betas[i]
         cfg.steps_out, cfg.k_src, cfg.k_obs = steps_out, self.e_rad, self.o_rad
+        cfg.option, cfg.npmlbot, cfg.npmltop = option, npmlbot, npmltop
         self.cfg = cfg
         h = ctypes.c_void_p()
         capi.check(self.L.sparc5_plan_create(ctypes.byref(cfg), ctypes.byref(h)), "sparc5_plan_create")

@@ -1,5 +1,6 @@
-"""2-D sponge solver (option 5, sparc5_*) against the CPU oracle of MP_QUIET_SPONGE_2D
-(oracle/sparc_oracle_sponge.c), and its FP32 plan against its FP64 plan."""
+"""2-D velocity-pressure-density solvers (option 5 with the sponge, option 6 with the PML,
+sparc5_*) against the CPU oracle of MP_QUIET_SPONGE_2D / MP_QUIET_PML_2D
+(oracle/sparc_oracle_sponge.c), and their FP32 plans against their FP64 plans."""
 import numpy as np
 import pytest
 
@@ -18,9 +19,10 @@ def _inputs(nb=2, nsteps=40):
     return M.polytrope(300), pats, np.sin(np.arange(nsteps + 5) * 0.3) * 1e-6
 
 
-def _gpu(precision, nsteps, nb=2):
+def _gpu(precision, nsteps, nb=2, option=5):
     model, pats, amp = _inputs(nb, nsteps)
-    ws = WaveSolverSponge(NX, model, XL, nbatch=nb, precision=precision, steps_out=15, obsheight_cm=-100e5)
+    ws = WaveSolverSponge(NX, model, XL, nbatch=nb, precision=precision, steps_out=15, obsheight_cm=-100e5,
+                          option=option)
     ws.set_source(pats, amp)
     ws.reset(0)
     seis = ws.forward(nsteps).double().cpu().numpy()
@@ -33,12 +35,13 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-def test_fp64_matches_oracle():
+@pytest.mark.parametrize("option", [5, 6])
+def test_fp64_matches_oracle(option):
     nsteps, nb = 31, 2
-    st, seis = _gpu(64, nsteps, nb)
+    st, seis = _gpu(64, nsteps, nb, option)
     model, pats, amp = _inputs(nb, nsteps)
     for b in range(nb):
-        s = SimSponge(NX, model, XL, steps_out=15, obsheight_cm=-100e5)
+        s = SimSponge(NX, model, XL, steps_out=15, obsheight_cm=-100e5, option=option)
         s.set_source(pats[b], amp)
         rec = s.run(nsteps)
         want = s.state()
@@ -50,9 +53,10 @@ def test_fp64_matches_oracle():
         assert rel(seis[:, b], rec) < 1e-10
 
 
-def test_fp32_tracks_fp64():
-    st32, s32 = _gpu(32, 60)
-    st64, s64 = _gpu(64, 60)
+@pytest.mark.parametrize("option", [5, 6])
+def test_fp32_tracks_fp64(option):
+    st32, s32 = _gpu(32, 60, option=option)
+    st64, s64 = _gpu(64, 60, option=option)
     for v in (0, 1, 3, 4):
         assert rel(st32[v], st64[v]) < 1e-4, (v, rel(st32[v], st64[v]))
 
