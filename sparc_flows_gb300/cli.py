@@ -9,6 +9,13 @@ chosen exactly as in READ_PARAMETERS:
   line 1 'adjoint'                         -> adjoint solve;
   no instruction file                      -> kernel construction (PRODUCE_KERNELS).
 Marker files in the working directory: compute_data, linesearch, compute_synth.
+Option: with KERNEL_MODE, READ_PARAMETERS sets option 17 whenever the instruction's second line is
+'2D' (initialize.f90:1094, 1135-1138), overriding PARSE_OPTIONS; the Spectral and Adjoint
+templates the callers copy carry that line, and option 17 is the solve run here.  Options 5 and 6
+are unreachable through the reference executable (TEST_IN_2D is only set by READ_PARAMETERS) and
+are the WaveSolverSponge API.  An instruction without '2D' selects option 16: with ny = 1 it is
+run as option 17 (the same equations with no y-dependence), with ny > 1 the executable exits with
+status 2 (the 3-D solver is the WaveSolver3D API).
 
 Files written (same names and FITS layout as the reference):
   <dir>/forward_srcNN_lsMM/{vz_cc.fits, timeline, kernel_info, rms_hist}
@@ -73,11 +80,16 @@ def main(argv=None) -> int:
         run = run.replace(nsteps=int(os.environ["SPARC_NSTEPS"]))
     precision = int(os.environ.get("SPARC_PRECISION", "64"))
     device = os.environ.get("SPARC_DEVICE", "cuda:0")
-    model = load_model(params.get("file_data", "solar_deep"), run.nz)
     instr = f"Instruction_src{contrib}_ls{jobno}"
+    kind, twod = _read_instruction(instr) if os.path.exists(instr) else ("", True)
+    if not twod and int(params.get("ny", 1)) > 1:
+        # no '2D' line and ny > 1: PARSE_OPTIONS picks the 3-D option 16 (initialize.f90:833-837),
+        # which this executable does not run -- the 3-D solver is the WaveSolver3D API
+        print("sparc: 3-D instruction (option 16) with ny > 1: use sparc_flows_gb300.solver3d", file=sys.stderr)
+        return 2
+    model = load_model(params.get("file_data", "solar_deep"), run.nz)
     compute_data = os.path.exists("compute_data")
     if os.path.exists(instr):
-        kind, _ = _read_instruction(instr)
         if kind == "spectral":
             rc = _forward(run, model, directory, contrib, jobno, src, precision, device, compute_data)
             if os.path.exists(instr):

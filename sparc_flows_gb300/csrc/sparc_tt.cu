@@ -14,9 +14,10 @@
 // one inverse 2-D transform of c.
 //
 // Fields are complex [nb][nt][nx] (x fastest).  x transforms: one warp per row, the shared-
-// memory Stockham FFT of the wave solver (nx in its table).  t transforms: any nt, direct DFT
-// over a 16-column tile held in shared memory (nt^2 nx operations per transform; nt is the
-// number of records, a few hundred).  FFTW's transforms are unnormalised, and so are these.
+// memory Stockham FFT of the wave solver (nx in its table).  t transforms: any nt (the record
+// count, 240 or 241 for 3600 steps -- 241 is prime): Bluestein's chirp-z transform on two
+// power-of-two FFTs of length M >= 2 nt - 1 (nt <= 512), a direct DFT over 16-column tiles above
+// that.  FFTW's transforms are unnormalised, and so are these.
 #include <cmath>
 #include <string>
 #include <vector>
@@ -92,6 +93,73 @@ __global__ void __launch_bounds__(TT_THREADS) tt_dft_t_kernel(double2 *data, int
             if (m >= nt) m -= nt;
         }
         if (x0 + c < nx) base[(size_t)k * nx + c] = make_double2(sr, si);
+    }
+}
+
+// t transform by Bluestein's chirp-z algorithm: nk = (n^2 + k^2 - (k-n)^2) / 2 turns the length-nt
+// DFT into a convolution with the chirp b_m = exp(+i pi m^2 / nt), evaluated with two power-of-two
+// FFTs of length M >= 2 nt - 1 (Bluestein, IEEE Trans. Audio Electroacoust. 18 (1970) 451-455):
+//   X_k = w_k IFFT_M( FFT_M(x_n w_n) * FFT_M(b) )_k / M,   w_n = exp(-i pi n^2 / nt).
+// The inverse transform is the conjugate of the forward one of the conjugate.  A block of WPB warps
+// takes WPB consecutive columns (b, x0 .. x0 + WPB - 1): the tile [nt][WPB] is loaded and stored
+// row-contiguously (WPB x 16 bytes per record) through shared memory, each warp transforms one
+// column with the Stockham FFT of the x transforms.
+template <int M, int WPB>
+__global__ void __launch_bounds__(WPB *WARP) tt_bluestein_t_kernel(double2 *data, int nt, int nx, const double2 *chirp,
+                                                                   const double2 *bhat, const double *twr,
+                                                                   const double *twi, int inverse)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *sm = reinterpret_cast<double *>(smem_raw);
+    constexpr int SW = 4 * M + 2;  // per-warp stride: the tile rows of 8 warps land on distinct banks
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int x0 = blockIdx.x * WPB;
+    double2 *base = data + (size_t)blockIdx.y * nt * nx + x0;
+    const double cs = inverse ? -1.0 : 1.0;  // conjugation of the input and output for the inverse
+    for (int idx = threadIdx.x; idx < nt * WPB; idx += WPB * WARP) {
+        const int t = idx / WPB, c = idx % WPB;
+        double *xr = sm + (size_t)c * SW, *xi = xr + M;
+        double2 v = (x0 + c < nx) ? base[(size_t)t * nx + c] : make_double2(0.0, 0.0);
+        v.y *= cs;
+        const double2 w = chirp[t];
+        xr[t] = v.x * w.x - v.y * w.y;
+        xi[t] = v.x * w.y + v.y * w.x;
+    }
+    double *xr = sm + (size_t)warp * SW, *xi = xr + M, *yr = xi + M, *yi = yr + M;
+    for (int t = nt + lane; t < M; t += WARP) {
+        xr[t] = 0.0;
+        xi[t] = 0.0;
+    }
+    __syncthreads();
+    double *fr, *fi;
+    FFTRun<double, M, 0, 1>::run(xr, xi, yr, yi, twr, twi, lane, false, 1.0, 1.0, fr, fi);
+    for (int k = lane; k < M; k += WARP) {
+        const double2 b = bhat[k];
+        const double ar = fr[k], ai = fi[k];
+        fr[k] = ar * b.x - ai * b.y;
+        fi[k] = ar * b.y + ai * b.x;
+    }
+    __syncwarp();
+    double *gr = (fr == xr) ? yr : xr, *gi = (fr == xr) ? yi : xi;
+    double *cr, *ci;
+    FFTRun<double, M, 0, 1>::run(fr, fi, gr, gi, twr, twi, lane, true, 1.0, 1.0, cr, ci);
+    __syncwarp();
+    const double inv_m = 1.0 / (double)M;
+    for (int k = lane; k < nt; k += WARP) {  // X_k = w_k c_k / M, back into the warp's own buffer
+        const double2 w = chirp[k];
+        const double ar = cr[k] * inv_m, ai = ci[k] * inv_m;
+        const double rr = ar * w.x - ai * w.y, ri = ar * w.y + ai * w.x;
+        cr[k] = rr;
+        ci[k] = ri * cs;
+    }
+    if (lane == 0) reinterpret_cast<int *>(sm + (size_t)WPB * SW)[warp] = (int)(cr - (sm + (size_t)warp * SW));
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nt * WPB; idx += WPB * WARP) {
+        const int t = idx / WPB, c = idx % WPB;
+        if (x0 + c >= nx) continue;
+        const double *wb = sm + (size_t)c * SW;
+        const int off = reinterpret_cast<const int *>(sm + (size_t)WPB * SW)[c];
+        base[(size_t)t * nx + c] = make_double2(wb[off + t], wb[off + M + t]);
     }
 }
 
@@ -343,6 +411,9 @@ struct sparc_tt_plan {
     double2 *wt = nullptr;
     TTRow *rows = nullptr;
     int cap = 0;
+    int bm = 0;  // Bluestein length (0: direct DFT along t)
+    double2 *chirp = nullptr, *bhat = nullptr;
+    double *btwr = nullptr, *btwi = nullptr;
 };
 
 namespace {
@@ -369,8 +440,28 @@ cudaError_t fft_x(sparc_tt_plan *p, double2 *f, int inverse, cudaStream_t st)
 
 size_t dft_t_smem(int nt) { return ((size_t)nt * TT_COLS + nt) * sizeof(double2); }
 
+template <int M, int WPB>
+cudaError_t bluestein_t(sparc_tt_plan *p, double2 *f, int inverse, cudaStream_t st)
+{
+    const size_t smem = (size_t)WPB * (4 * M + 2) * sizeof(double) + WPB * sizeof(int) + 16;
+    auto k = tt_bluestein_t_kernel<M, WPB>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((p->nx + WPB - 1) / WPB, p->nb);
+    k<<<grid, WPB * WARP, smem, st>>>(f, p->nt, p->nx, p->chirp, p->bhat, p->btwr, p->btwi, inverse);
+    return cudaGetLastError();
+}
+
 cudaError_t dft_t(sparc_tt_plan *p, double2 *f, int inverse, cudaStream_t st)
 {
+    switch (p->bm) {
+        case 64: return bluestein_t<64, 8>(p, f, inverse, st);
+        case 128: return bluestein_t<128, 8>(p, f, inverse, st);
+        case 256: return bluestein_t<256, 8>(p, f, inverse, st);
+        case 512: return bluestein_t<512, 8>(p, f, inverse, st);
+        case 1024: return bluestein_t<1024, 4>(p, f, inverse, st);
+        default: break;
+    }
     const size_t smem = dft_t_smem(p->nt);
     cudaError_t e = cudaFuncSetAttribute(tt_dft_t_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -444,6 +535,47 @@ int sparc_tt_plan_create(int nx, int nt, int nbatch, int max_rows, sparc_tt_plan
     if (e == cudaSuccess) e = cudaMemcpy(p->twi, ti.data(), nx * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(p->wt, w.data(), nt * sizeof(double2), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(p->adj, 0, n * sizeof(double));
+    // Bluestein tables: the smallest power of two M >= 2 nt - 1 in the FFT table (64..1024)
+    int M = 64;
+    while (M < 2 * nt - 1) M *= 2;
+    if (e == cudaSuccess && M <= 1024) {
+        p->bm = M;
+        std::vector<double2> ch(nt), bext(M, make_double2(0.0, 0.0)), bh(M);
+        std::vector<double> btr(M), bti(M);
+        for (int m = 0; m < nt; m++) {
+            // n^2 mod 2 nt keeps the phase argument small (exp(-i pi n^2 / nt) has period 2 nt in n^2)
+            const long long q = ((long long)m * m) % (2LL * nt);
+            const double ang = TT_PI * (double)q / (double)nt;
+            ch[m] = make_double2(std::cos(ang), -std::sin(ang));
+            bext[m] = make_double2(std::cos(ang), std::sin(ang));
+            if (m > 0) bext[M - m] = bext[m];
+        }
+        for (int t = 0; t < M; t++) {
+            btr[t] = std::cos(2.0 * TT_PI * (double)t / (double)M);
+            bti[t] = -std::sin(2.0 * TT_PI * (double)t / (double)M);
+        }
+        for (int k = 0; k < M; k++) {  // FFT_M(b) by a direct sum on the host (once per plan)
+            double sr = 0.0, si = 0.0;
+            for (int m = 0; m < M; m++) {
+                const long long q = ((long long)k * m) % M;
+                const double c = btr[q], sn = bti[q];
+                sr += bext[m].x * c - bext[m].y * sn;
+                si += bext[m].x * sn + bext[m].y * c;
+            }
+            bh[k] = make_double2(sr, si);
+        }
+        struct Req2 { void **ptr; size_t bytes; };
+        Req2 r2[4] = {{(void **)&p->chirp, nt * sizeof(double2)}, {(void **)&p->bhat, M * sizeof(double2)},
+                      {(void **)&p->btwr, M * sizeof(double)}, {(void **)&p->btwi, M * sizeof(double)}};
+        for (auto &r : r2) {
+            if (e == cudaSuccess) e = cudaMalloc(r.ptr, r.bytes);
+            if (e == cudaSuccess) p->allocs.push_back(*r.ptr);
+        }
+        if (e == cudaSuccess) e = cudaMemcpy(p->chirp, ch.data(), nt * sizeof(double2), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(p->bhat, bh.data(), M * sizeof(double2), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(p->btwr, btr.data(), M * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(p->btwi, bti.data(), M * sizeof(double), cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess) {
         sparc_tt_plan_destroy(p);
         return tt_fail("sparc_tt_plan_create: tables", e);

@@ -53,3 +53,16 @@ def test_instruction_files(tmp_path):
         f.write_text(f"{kind}\n2D\n" + ("T\n" if kind == "spectral" else ""))
         k, twod = _read_instruction(str(f))
         assert k == kind and twod
+
+
+def test_cli_refuses_3d_instruction(tmp_path, monkeypatch):
+    """An instruction without the '2D' line selects option 16 (initialize.f90:833-837, 1094); with
+    ny > 1 the executable exits with status 2 before touching a model file or the GPU."""
+    from sparc_flows_gb300 import cli
+    text = GOLD["params_i"].replace("ny = 1", "ny = 64")
+    assert text != GOLD["params_i"]
+    (tmp_path / "params.i").write_text(text)
+    (tmp_path / "Instruction_src01_ls00").write_text("spectral\n3D\n")
+    monkeypatch.chdir(tmp_path)
+    assert cli.main(["01", "00"]) == 2
+    assert (tmp_path / "Instruction_src01_ls00").exists()

@@ -82,3 +82,20 @@ def test_misfit_all_matches_oracle():
     for fb in range(3):
         assert np.allclose(again[fb]["misfit"], bands[fb]["misfit"], rtol=1e-12)
     tt.close()
+
+
+@pytest.mark.parametrize("nt", [37, 241, 520])
+def test_record_counts(nt):
+    """Both t transforms: Bluestein's chirp-z (nt <= 512; 241 is prime) and the direct DFT (nt > 512)."""
+    rng = np.random.default_rng(nt)
+    s = rng.standard_normal((1, nt, NX))
+    d = np.roll(s, 1, axis=1) + 0.05 * rng.standard_normal(s.shape)
+    tmin = -(CAD * (np.arange(nt) + 1.0))[::-1] / 60.0
+    modes = {0: (3.0, 20.0, 10.0)}
+    tt = TT.TTAdjoint(NX, nt, 1, XL, CAD)
+    res = tt.run(torch.as_tensor(s, device="cuda"), torch.as_tensor(d, device="cuda"), [0.0], tmin, modes)
+    tt.close()
+    ref = TO.adjoint_source(s[0], d[0], 0.0, XL, tmin, CAD, modes)
+    assert res["nmeas"][0] == ref["nmeas"] > 0
+    adj = res["adj"][0].cpu().numpy()
+    assert np.linalg.norm(adj - ref["adj"]) <= 1e-10 * np.linalg.norm(ref["adj"])
