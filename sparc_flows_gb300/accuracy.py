@@ -42,4 +42,10 @@ def fp32_vs_fp64(workload: str = "batch32", source: int = 15, nsteps: int | None
     for name in k64:
         rep[name] = rel_l2(k32[name], k64[name])
     rep["max"] = max(v for k, v in rep.items() if k not in ("workload", "source_x_mm", "nsteps"))
+    # the same over the physical interior: rows and columns of the absorbing layers left out
+    zs = slice(run.npmlbot, run.nz - run.npmltop)
+    xs = slice(run.npmlhor, run.nx - run.npmlhor)
+    inner = {name: rel_l2(k32[name][zs, xs], k64[name][zs, xs]) for name in k64}
+    inner["max"] = max(inner.values())
+    rep["interior"] = dict(rows=[zs.start, zs.stop], columns=[xs.start, xs.stop], **inner)
     return rep
