@@ -386,6 +386,25 @@ def run_gpu(args):
     e2e_ms = float(te.item())
     e2e_value = pipe.point_steps() * e2e_steps * world / (e2e_ms * 1e-3)
 
+    # ---- the same batch with the forward field checkpointed in HBM every 16 records and recomputed
+    # per segment during the adjoint run (one run after a warm-up; kernels equal the stored run's)
+    checkpointed = None
+    if rank == 0 and not args.no_checkpoint:
+        ckp = FwdAdjKernels(run, model, specs, psi=psi, cmul=cmul, precision=32, device=dev, checkpoint_every=16)
+        ckp.run_all()
+        torch.cuda.synchronize()
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        ckp.run_all()
+        c1.record(stream)
+        torch.cuda.synchronize()
+        cms = c0.elapsed_time(c1)
+        checkpointed = {"every_records": 16, "value": ckp.point_steps() / (cms * 1e-3), "unit": UNIT,
+                        "ms_per_run": cms, "forward_solves_per_run": 2,
+                        "partial_state_bytes": ckp.snaps.numel() * ckp.snaps.element_size() + ckp.ckpt.numel(),
+                        "stored_partial_state_bytes": pipe.snaps.numel() * pipe.snaps.element_size()}
+        ckp.close()
+
     # ---- accuracy of the FP32 batched path against FP64 on one source of the same workload
     accuracy = None
     if rank == 0 and not args.no_accuracy:
@@ -428,6 +447,8 @@ def run_gpu(args):
             line["fp64_plain"] = plain
         if accuracy is not None:
             line["accuracy"] = accuracy
+        if checkpointed is not None:
+            line["checkpointed"] = checkpointed
         if not args.no_gradient:
             line["gradient"] = gradient_stage(pipe, model, dev, cpu=not args.no_cpu)
             line["tt_adjoint_source"] = tt_stage(seis_h.to(dev), run, specs, dev, cpu=not args.no_cpu)
@@ -559,6 +580,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain reference path")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy report")
     ap.add_argument("--no-gradient", action="store_true", help="skip the gradient post-processing figures")
+    ap.add_argument("--no-checkpoint", action="store_true", help="skip the checkpointed-run figures")
     ap.add_argument("--autotune", action="store_true", help="uneven48: time column-pass variants per group first")
     ap.add_argument("--workload", default="batch32", choices=["batch32", "uneven48", "3d4"],
                     help="uneven48: 48 solves of mixed grids, lengths and backgrounds (seed 0)")

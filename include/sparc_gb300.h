@@ -128,6 +128,22 @@ int sparc_reset_state(sparc_plan_t *plan, int time0, void *stream);
 int sparc_forward(sparc_plan_t *plan, int nsteps, double flow_sign, void *seis, void *snaps,
                   int nrec_cap, int use_graph, void *stream);
 
+/* sparc_forward with a record window: records rec0 .. rec0 + nrec_cap - 1 (the record index is
+ * time/steps_out) go to slots 0 .. nrec_cap - 1 of seis / snaps; others are dropped.  With a
+ * checkpoint (below) this recomputes one segment of a forward run's partial states
+ * (all_modules.f90:750-784) into a buffer of nrec_cap records instead of keeping them all. */
+int sparc_forward_window(sparc_plan_t *plan, int nsteps, double flow_sign, void *seis, void *snaps, int rec0,
+                         int nrec_cap, int use_graph, void *stream);
+
+/* Checkpoint of everything a step carries to the next: the step counter, the state, the
+ * compensated low parts (if any) and the PML auxiliaries of every solve.  The reference has none
+ * (it restarts from its partial-state dumps); here the forward field is checkpointed in DEVICE
+ * memory every few records and recomputed per segment during the adjoint run.  save / load copy
+ * sparc_checkpoint_bytes(plan) bytes to / from a 16-byte aligned DEVICE buffer (stream-ordered). */
+size_t sparc_checkpoint_bytes(const sparc_plan_t *plan);
+int sparc_checkpoint_save(sparc_plan_t *plan, void *dst, void *stream);
+int sparc_checkpoint_load(sparc_plan_t *plan, const void *src, void *stream);
+
 /* The state of solve b: copy the four live fields (xi_x, xi_z, v_x, v_z), each nz*nx of the
  * plan precision, to or from DEVICE memory (for checkpoints and tests). */
 int sparc_get_state(sparc_plan_t *plan, void *dst, void *stream);

@@ -31,6 +31,11 @@ SIGNATURES = {
     "sparc_set_source": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _dp, _ip, ctypes.c_int, _vp]),
     "sparc_reset_state": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
     "sparc_forward": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "sparc_forward_window": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, _vp]),
+    "sparc_checkpoint_bytes": (ctypes.c_size_t, [_vp]),
+    "sparc_checkpoint_save": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc_checkpoint_load": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_set_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_profile_passes": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _vp]),

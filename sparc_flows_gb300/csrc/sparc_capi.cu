@@ -5,6 +5,7 @@
 // a CUDA graph and replayed once per step.
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -513,7 +514,7 @@ struct sparc_plan {
     cudaGraphExec_t gexec = nullptr;
     cudaGraph_t graph = nullptr;
     const void *g_seis = nullptr, *g_snaps = nullptr;
-    int g_cap = -1;
+    int g_cap = -1, g_rec0 = 0;
     double g_fsign = 0.0;
     cudaStream_t g_stream = nullptr;
     double *d_srcw = nullptr;
@@ -791,7 +792,7 @@ int profile_passes(sparc_plan *p, int nsteps, double *ms, cudaStream_t st)
 }
 
 template <typename T>
-int run_forward(sparc_plan *p, int nsteps, double fsign, void *seis, void *snaps, int cap, int use_graph,
+int run_forward(sparc_plan *p, int nsteps, double fsign, void *seis, void *snaps, int rec0, int cap, int use_graph,
                 cudaStream_t st)
 {
     Solver<T> &S = solver<T>(p);
@@ -800,13 +801,14 @@ int run_forward(sparc_plan *p, int nsteps, double fsign, void *seis, void *snaps
     a.seis = (T *)seis;
     a.snaps = (T *)snaps;
     a.nrec_cap = cap;
+    a.rec0 = rec0;
     a.unstretch_top = (T)p->unstretch_top;
     if (!use_graph) {
         for (int i = 0; i < nsteps; i++) CK(enqueue_step<T>(p, a, st));
         return SPARC_OK;
     }
     const bool same = p->gexec && p->g_seis == seis && p->g_snaps == snaps && p->g_cap == cap &&
-                      p->g_fsign == fsign && p->g_stream == st;
+                      p->g_rec0 == rec0 && p->g_fsign == fsign && p->g_stream == st;
     if (!same) {
         if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
         if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
@@ -822,7 +824,7 @@ int run_forward(sparc_plan *p, int nsteps, double fsign, void *seis, void *snaps
         if (e2 != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
         p->graph = g;
         CK(cudaGraphInstantiate(&p->gexec, g, 0));
-        p->g_seis = seis; p->g_snaps = snaps; p->g_cap = cap; p->g_fsign = fsign; p->g_stream = st;
+        p->g_seis = seis; p->g_snaps = snaps; p->g_cap = cap; p->g_rec0 = rec0; p->g_fsign = fsign; p->g_stream = st;
     }
     for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(p->gexec, st));
     return SPARC_OK;
@@ -918,6 +920,38 @@ int reset_state(sparc_plan *p, int time0, cudaStream_t st)
     CK(cudaMemcpyAsync(p->d_time, &tm1, sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
     return SPARC_OK;
+}
+
+// Checkpoint layout: the step counter (16 bytes), then the persistent device state of the batch
+// in this order -- A [nb][4][nz][nx], ALO (compensated FP32 plans only, same shape), PZ
+// [nb][2][nzpml][nx], PX [nb][2][nz][2 npmlhor] -- all of the plan precision.  The RHS registers
+// (SV, SPZ, SPX) are not part of it: stage 1 of a step reads none of them.
+struct CkptPart {
+    void *ptr;
+    size_t bytes;
+};
+
+template <typename T>
+int checkpoint_parts(sparc_plan *p, CkptPart (&parts)[4])
+{
+    Solver<T> &S = solver<T>(p);
+    const sparc_config_t &c = p->cfg;
+    const size_t nb = c.nbatch, F = S.F, nzpml = c.npmlbot + c.npmltop, nhx = 2 * c.npmlhor;
+    parts[0] = {S.a.A, nb * 4 * F * sizeof(T)};
+    parts[1] = {S.a.ALO, S.a.ALO ? nb * 4 * F * sizeof(T) : 0};
+    parts[2] = {S.a.PZ, nb * 2 * nzpml * c.nx * sizeof(T)};
+    parts[3] = {S.a.PX, nb * 2 * c.nz * nhx * sizeof(T)};
+    return 4;
+}
+
+size_t checkpoint_bytes(sparc_plan *p)
+{
+    CkptPart parts[4];
+    if (p->cfg.precision == 32) checkpoint_parts<float>(p, parts);
+    else checkpoint_parts<double>(p, parts);
+    size_t n = 16;
+    for (auto &q : parts) n += q.bytes;
+    return n;
 }
 
 bool check_cfg(const sparc_config_t *c, std::string &why)
@@ -1063,8 +1097,61 @@ int sparc_forward(sparc_plan_t *p, int nsteps, double flow_sign, void *seis, voi
     if (!p->have_bg || !p->have_src) return fail(SPARC_ERR_STATE, "sparc_forward: background and source must be set first");
     if (nrec_cap > 0 && !seis && !snaps) return fail(SPARC_ERR_ARG, "sparc_forward: nrec_cap without outputs");
     return p->cfg.precision == 32
-               ? run_forward<float>(p, nsteps, flow_sign, seis, snaps, nrec_cap, use_graph, (cudaStream_t)stream)
-               : run_forward<double>(p, nsteps, flow_sign, seis, snaps, nrec_cap, use_graph, (cudaStream_t)stream);
+               ? run_forward<float>(p, nsteps, flow_sign, seis, snaps, 0, nrec_cap, use_graph, (cudaStream_t)stream)
+               : run_forward<double>(p, nsteps, flow_sign, seis, snaps, 0, nrec_cap, use_graph, (cudaStream_t)stream);
+}
+
+int sparc_forward_window(sparc_plan_t *p, int nsteps, double flow_sign, void *seis, void *snaps, int rec0,
+                         int nrec_cap, int use_graph, void *stream)
+{
+    if (!p || nsteps < 0 || nrec_cap < 0 || rec0 < 0) return fail(SPARC_ERR_ARG, "sparc_forward_window: bad argument");
+    if (!p->have_bg || !p->have_src)
+        return fail(SPARC_ERR_STATE, "sparc_forward_window: background and source must be set first");
+    if (nrec_cap > 0 && !seis && !snaps) return fail(SPARC_ERR_ARG, "sparc_forward_window: nrec_cap without outputs");
+    return p->cfg.precision == 32
+               ? run_forward<float>(p, nsteps, flow_sign, seis, snaps, rec0, nrec_cap, use_graph, (cudaStream_t)stream)
+               : run_forward<double>(p, nsteps, flow_sign, seis, snaps, rec0, nrec_cap, use_graph, (cudaStream_t)stream);
+}
+
+size_t sparc_checkpoint_bytes(const sparc_plan_t *p)
+{
+    return p ? checkpoint_bytes(const_cast<sparc_plan_t *>(p)) : 0;
+}
+
+int sparc_checkpoint_save(sparc_plan_t *p, void *dst, void *stream)
+{
+    if (!p || !dst) return fail(SPARC_ERR_ARG, "sparc_checkpoint_save: bad argument");
+    if ((reinterpret_cast<uintptr_t>(dst) & 15) != 0) return fail(SPARC_ERR_ARG, "sparc_checkpoint_save: dst not 16-byte aligned");
+    CkptPart parts[4];
+    if (p->cfg.precision == 32) checkpoint_parts<float>(p, parts);
+    else checkpoint_parts<double>(p, parts);
+    cudaStream_t st = (cudaStream_t)stream;
+    char *d = static_cast<char *>(dst);
+    CK(cudaMemcpyAsync(d, p->d_time, sizeof(int), cudaMemcpyDeviceToDevice, st));
+    d += 16;
+    for (auto &q : parts) {
+        if (q.bytes) CK(cudaMemcpyAsync(d, q.ptr, q.bytes, cudaMemcpyDeviceToDevice, st));
+        d += q.bytes;
+    }
+    return SPARC_OK;
+}
+
+int sparc_checkpoint_load(sparc_plan_t *p, const void *src, void *stream)
+{
+    if (!p || !src) return fail(SPARC_ERR_ARG, "sparc_checkpoint_load: bad argument");
+    if ((reinterpret_cast<uintptr_t>(src) & 15) != 0) return fail(SPARC_ERR_ARG, "sparc_checkpoint_load: src not 16-byte aligned");
+    CkptPart parts[4];
+    if (p->cfg.precision == 32) checkpoint_parts<float>(p, parts);
+    else checkpoint_parts<double>(p, parts);
+    cudaStream_t st = (cudaStream_t)stream;
+    const char *d = static_cast<const char *>(src);
+    CK(cudaMemcpyAsync(p->d_time, d, sizeof(int), cudaMemcpyDeviceToDevice, st));
+    d += 16;
+    for (auto &q : parts) {
+        if (q.bytes) CK(cudaMemcpyAsync(q.ptr, d, q.bytes, cudaMemcpyDeviceToDevice, st));
+        d += q.bytes;
+    }
+    return SPARC_OK;
 }
 
 int sparc_profile_passes(sparc_plan_t *p, int nsteps, double *ms, void *stream)

@@ -328,8 +328,8 @@ __global__ void __launch_bounds__(CW *ColCfg<T>::MAXNCH, (min_blocks<T, CW>())) 
     const size_t F = (size_t)nz * nx;
     T *Ab = a.A + (size_t)b * 4 * F;
     const int time = *a.d_time;
-    const int rec = (a.steps_out > 0) ? time / a.steps_out : 0;
-    const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec < a.nrec_cap && time >= 0;
+    const int rec = (a.steps_out > 0) ? time / a.steps_out - a.rec0 : 0;  // slot in the record window
+    const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec >= 0 && rec < a.nrec_cap && time >= 0;
     const bool xf = a.filt_xall || ((x >= a.nh - 1) && (x <= nx - a.nh));
     T *snap = record && a.snaps ? a.snaps + ((size_t)b * a.nrec_cap + rec) * 6 * F : nullptr;
     if constexpr (sizeof(T) == 4) {

@@ -72,6 +72,7 @@ struct StepArgs {
     int ntab;
     T *seis, *snaps;
     int nrec_cap;
+    int rec0;  // records rec0 .. rec0 + nrec_cap - 1 are written, to slots 0 .. nrec_cap - 1
 };
 
 template <typename T>

@@ -41,8 +41,8 @@ __global__ void __launch_bounds__(END_CW *END_WARPS) end_step_stream_kernel(Step
     const int p = blockIdx.y & 1, b = blockIdx.y >> 1;  // component (0: x, 1: z), solve
     const size_t F = (size_t)nz * nx;
     const int time = *a.d_time;
-    const int rec = (a.steps_out > 0) ? time / a.steps_out : 0;
-    const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec < a.nrec_cap && time >= 0;
+    const int rec = (a.steps_out > 0) ? time / a.steps_out - a.rec0 : 0;  // slot in the record window
+    const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec >= 0 && rec < a.nrec_cap && time >= 0;
     T *snap = record && a.snaps ? a.snaps + ((size_t)b * a.nrec_cap + rec) * 6 * F : nullptr;
     const T *Axi = a.A + ((size_t)b * 4 + p) * F, *Av = a.A + ((size_t)b * 4 + 2 + p) * F;
     const T *R4 = svp(a, a.slot_sm1, b, p), *R5 = svp(a, a.slot_s, b, p);
@@ -168,8 +168,8 @@ __global__ void __launch_bounds__(ENDC_CW *ENDC_ROWS) end_step_comp_kernel(StepA
     const int p = blockIdx.y & 1, b = blockIdx.y >> 1;  // component (0: x, 1: z), solve
     const size_t F = (size_t)nz * nx;
     const int time = *a.d_time;
-    const int rec = (a.steps_out > 0) ? time / a.steps_out : 0;
-    const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec < a.nrec_cap && time >= 0;
+    const int rec = (a.steps_out > 0) ? time / a.steps_out - a.rec0 : 0;  // slot in the record window
+    const bool record = a.steps_out > 0 && time % a.steps_out == 0 && rec >= 0 && rec < a.nrec_cap && time >= 0;
     float *snap = record && a.snaps ? a.snaps + ((size_t)b * a.nrec_cap + rec) * 6 * F : nullptr;
     float *Axi = a.A + ((size_t)b * 4 + p) * F, *Av = a.A + ((size_t)b * 4 + 2 + p) * F;
     float *Lxig = a.ALO + ((size_t)b * 4 + p) * F, *Lvg = a.ALO + ((size_t)b * 4 + 2 + p) * F;

@@ -4,7 +4,10 @@ instruction, with the Adjoint instruction, then without one (kernel stage) -- do
 with every wavefield resident in HBM instead of ~520 partial-state FITS dumps.
 
 Forward partial states are kept in device memory at the reference cadence (every
-steps_out steps, all_modules.f90:750-784).  The adjoint is the reference's continuous adjoint: a
+steps_out steps, all_modules.f90:750-784): all of them, or with ``checkpoint_every=K`` only a
+checkpoint of the forward solve every K records and a buffer of K records, each segment being
+recomputed from its checkpoint when the adjoint run reaches it (one more forward solve for about
+K/nrec of the memory).  The adjoint is the reference's continuous adjoint: a
 forward-type solve with the flow negated (driver.f90:144-147) driven by the time-reversed
 residual injected at o_rad (physics2d.f90:1052-1054).  After each adjoint step that produces a
 record, its v_x, v_z are paired with the matching forward record (kernels.f90:215, 258) and the
@@ -38,8 +41,12 @@ class FwdAdjKernels:
 
     def __init__(self, run: RunConfig, model: np.ndarray, specs: list[SourceSpec], psi=None, cmul=None,
                  precision: int = 32, receivers: np.ndarray | None = None, device: str = "cuda:0",
-                 column_impl: int | None = None, column_block: int | None = None):
+                 column_impl: int | None = None, column_block: int | None = None,
+                 checkpoint_every: int | None = None):
         self.run, self.nb = run, len(specs)
+        self.ck = int(checkpoint_every) if checkpoint_every else 0
+        if self.ck < 0 or self.ck >= run.nrec:
+            raise ValueError(f"checkpoint_every must be in 1..{run.nrec - 1}")
         self.dev = torch.device(device)
         col = dict(column_impl=column_impl, column_block=column_block)
         self.fwd = WaveSolver(run, model, nbatch=self.nb, precision=precision, cmul=cmul, psi=psi, device=device, **col)
@@ -49,12 +56,18 @@ class FwdAdjKernels:
         self.nrec = run.nrec
         self.rcv = receiver_columns(run) if receivers is None else np.asarray(receivers)
         dt = self.fwd.dtype
+        nbuf = self.ck or self.nrec
         with torch.cuda.device(self.dev):
             self.seis = torch.zeros((self.nb, self.nrec, run.nx), dtype=dt, device=self.dev)
-            self.snaps = torch.zeros((self.nb, self.nrec, 6, run.nz, run.nx), dtype=dt, device=self.dev)
+            self.snaps = torch.zeros((self.nb, nbuf, 6, run.nz, run.nx), dtype=dt, device=self.dev)
+            if self.ck:
+                nseg = -(-self.nrec // self.ck)
+                row = -(-self.fwd.checkpoint_bytes() // 256) * 256  # each checkpoint 256-byte aligned
+                self.ckpt = torch.empty((nseg, row), dtype=torch.uint8, device=self.dev)
             self.kacc = torch.zeros((self.nb, 4, run.nz, run.nx), dtype=torch.float64, device=self.dev)
             self.rcv_t = torch.as_tensor(self.rcv, device=self.dev)
         self._adj_src = None
+        self._seg = None  # segment whose forward records are in the buffer (checkpointed runs)
 
     def adjoint_source(self, data: torch.Tensor | None) -> torch.Tensor:
         """Waveform residual (synthetic minus data) at the receiver columns, time reversed, as the
@@ -66,10 +79,32 @@ class FwdAdjKernels:
         src[:, :, self.rcv_t] = torch.flip(res[:, :, self.rcv_t], dims=[1])
         return src
 
+    def _segment_steps(self, m: int) -> int:
+        """Steps of segment m: those from the step that writes record m*K up to the next segment's."""
+        so = self.run.steps_out
+        return min((m + 1) * self.ck * so, self.run.nsteps) - m * self.ck * so
+
     def forward(self):
         self.fwd.reset(0)
-        self.fwd.run_steps(self.run.nsteps, self.seis, self.snaps, self.nrec)
+        self._seg = None
+        if not self.ck:
+            self.fwd.run_steps(self.run.nsteps, self.seis, self.snaps, self.nrec)
+            return self.seis
+        for m in range(self.ckpt.shape[0]):
+            self.fwd.checkpoint_save(self.ckpt[m])
+            self.fwd.run_steps(self._segment_steps(m), self.seis, None, self.nrec)
         return self.seis
+
+    def _forward_records(self, jf: int):
+        """(buffer, slot) holding forward record jf, recomputing its segment from the checkpoint."""
+        if not self.ck:
+            return self.snaps, jf
+        m = jf // self.ck
+        if self._seg != m:
+            self.fwd.checkpoint_load(self.ckpt[m])
+            self.fwd.run_steps(self._segment_steps(m), None, self.snaps, self.ck, rec0=m * self.ck)
+            self._seg = m
+        return self.snaps, jf - m * self.ck
 
     def adjoint(self, src: torch.Tensor):
         """Adjoint solve with kernel accumulation at each record (kernels.f90:209-358)."""
@@ -82,7 +117,8 @@ class FwdAdjKernels:
             n = 1 if ja == 0 else so
             self.adj.run_steps(n, None, None, 0)
             done += n
-            self.adj.kernels_accumulate(self.snaps, self.nrec - 1 - ja, self.kacc)
+            buf, slot = self._forward_records(self.nrec - 1 - ja)
+            self.adj.kernels_accumulate(buf, slot, self.kacc)
         if run.nsteps > done:
             self.adj.run_steps(run.nsteps - done, None, None, 0)
 
@@ -95,7 +131,8 @@ class FwdAdjKernels:
     def launch_count(self) -> int:
         """Kernels of ours launched by one run_all."""
         per = WaveSolver.LAUNCHES_PER_STEP
-        return 2 * per * self.run.nsteps + 2 * self.nrec + 4
+        solves = 3 if self.ck else 2  # the checkpointed run recomputes the forward solve once
+        return solves * per * self.run.nsteps + 2 * self.nrec + 4
 
     def point_steps(self) -> int:
         """Grid-point steps of one run_all (forward and adjoint counted once each)."""

@@ -337,14 +337,31 @@ class WaveSolver:
         capi.check(self.L.sparc_reset_state(self.plan, time0, _stream()), "sparc_reset_state")
 
     def run_steps(self, nsteps: int, seis: torch.Tensor | None = None, snaps: torch.Tensor | None = None,
-                  nrec_cap: int | None = None, flow_sign: float | None = None, use_graph: bool = True):
-        """Advance nsteps steps; records go to the given device tensors."""
+                  nrec_cap: int | None = None, flow_sign: float | None = None, use_graph: bool = True,
+                  rec0: int = 0):
+        """Advance nsteps steps; records rec0 .. rec0 + nrec_cap - 1 go to the given device tensors
+        (slots 0 .. nrec_cap - 1)."""
         if flow_sign is None:
             flow_sign = -1.0 if self.run.adjoint else 1.0
         cap = nrec_cap if nrec_cap is not None else (seis.shape[1] if seis is not None else
                                                      (snaps.shape[1] if snaps is not None else 0))
-        capi.check(self.L.sparc_forward(self.plan, nsteps, flow_sign, _ptr(seis), _ptr(snaps), cap,
-                                        int(use_graph), _stream()), "sparc_forward")
+        if rec0:
+            capi.check(self.L.sparc_forward_window(self.plan, nsteps, flow_sign, _ptr(seis), _ptr(snaps), rec0, cap,
+                                                   int(use_graph), _stream()), "sparc_forward_window")
+        else:
+            capi.check(self.L.sparc_forward(self.plan, nsteps, flow_sign, _ptr(seis), _ptr(snaps), cap,
+                                            int(use_graph), _stream()), "sparc_forward")
+
+    def checkpoint_bytes(self) -> int:
+        """Bytes of one checkpoint (step counter, state, PML auxiliaries of the batch)."""
+        return int(self.L.sparc_checkpoint_bytes(self.plan))
+
+    def checkpoint_save(self, buf: torch.Tensor):
+        """Copy everything the next step depends on into the device byte buffer buf (16-byte aligned)."""
+        capi.check(self.L.sparc_checkpoint_save(self.plan, _ptr(buf), _stream()), "sparc_checkpoint_save")
+
+    def checkpoint_load(self, buf: torch.Tensor):
+        capi.check(self.L.sparc_checkpoint_load(self.plan, _ptr(buf), _stream()), "sparc_checkpoint_load")
 
     def forward(self, nsteps: int | None = None, snapshots: bool = False, use_graph: bool = True):
         """Run from rest: returns seismograms (nb, nrec, nx) and optionally snapshots
