@@ -203,6 +203,15 @@ int sparc_kernels_accumulate_static(sparc_plan_t *plan, const void *fsn, int nfw
 int sparc_zband_host(int nz, int ibc, const double *b, double *x, const double *preset, int n1,
                      double *band_err);
 
+/* Dense column operator for the discrete adjoint of the step (FP64, DEVICE pointers): for each
+ * of nb planes [nz][nx], out[k][j] = sum_m W[k][m] in[m][j] for columns i0 <= j <= i1 and
+ * out[k][j] = in[k][j] for the others; accumulate != 0 adds to out instead.  W is [nz][nz]
+ * row-major; in and out must not alias.  With W the transpose of a tabulated ddz (dbyd2.f:8-235
+ * times stretch, derivatives.f90:10-24) or of FILTER_VARS_2D's z filter (physics2d.f90:509-583),
+ * this applies the adjoint of that operator. */
+int sparc_colmat_apply(const double *W, int nz, const double *in, double *out, int nb, int nx, int i0, int i1,
+                       int accumulate, void *stream);
+
 /* Host-only FP64 evaluation of the partitioned compact-derivative algebra that the device
  * code applies (no GPU needed): x[nz][n1] = dbyd2(b, ibc) without the stretch factor, with
  * the same chunking as a plan whose chunks hold at most lmax rows.  For validating the

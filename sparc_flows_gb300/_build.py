@@ -15,7 +15,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB_PATH = os.path.join(OUT_DIR, "libsparc_gb300.so")
-SOURCES = ["sparc_row.cu", "sparc_col.cu", "sparc_col_tma.cu", "sparc_col_band.cu", "sparc_col_band_tma.cu", "sparc_end.cu", "sparc_capi.cu", "sparc_noalloc.cu", "sparc_grad.cu", "sparc_3d.cu", "sparc_tt.cu", "sparc_fits.cu", "sparc_sponge.cu"]
+SOURCES = ["sparc_row.cu", "sparc_col.cu", "sparc_col_tma.cu", "sparc_col_band.cu", "sparc_col_band_tma.cu", "sparc_end.cu", "sparc_capi.cu", "sparc_noalloc.cu", "sparc_grad.cu", "sparc_3d.cu", "sparc_tt.cu", "sparc_fits.cu", "sparc_sponge.cu", "sparc_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-I", CSRC, "-I", os.path.join(ROOT, "include")]

@@ -15,12 +15,17 @@ exactly the reference's adjoint + kernel stage.  The reference's adjoint is a co
 (time-reversal) adjoint: kernel_psi equals dL/dpsi up to the reference's fixed normalisation
 (its dimensional units) and the discretisation error of the continuous adjoint, which is what
 its line searches rely on.  ``fd_check`` measures both against central finite differences.
+
+The exact gradient of the same seismograms is ``exact_records`` (discrete_adjoint.py): its
+backward is the transpose of the device step itself, replayed from HBM checkpoints, and agrees
+with central finite differences to rounding.
 """
 from __future__ import annotations
 
 import numpy as np
 import torch
 
+from .discrete_adjoint import ExactGradient, records as exact_records  # noqa: F401
 from .pipeline import FwdAdjKernels
 
 

@@ -34,6 +34,8 @@ SIGNATURES = {
     "sparc_forward_window": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, _vp]),
     "sparc_checkpoint_bytes": (ctypes.c_size_t, [_vp]),
+    "sparc_colmat_apply": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, _vp]),
     "sparc_checkpoint_save": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_checkpoint_load": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
