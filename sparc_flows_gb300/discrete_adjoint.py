@@ -31,8 +31,6 @@ transposed filter is one of the plan's kernels.
 """
 from __future__ import annotations
 
-import ctypes
-
 import numpy as np
 import torch
 
@@ -266,8 +264,9 @@ class ExactGradient:
     step; states are checkpointed every `segment` steps in HBM and each segment is replayed once
     during the backward pass."""
 
-    def __init__(self, ws: WaveSolver, receivers, segment: int = 25):
+    def __init__(self, ws: WaveSolver, receivers, segment: int = 25, use_graph: bool = True):
         self.ws, self.ops = ws, StepOperators(ws)
+        self.use_graph, self._graph = use_graph, None
         self.run = ws.run
         self.rcv = torch.as_tensor(np.asarray(receivers), device=ws.dev)
         self.seg = int(segment)
@@ -315,17 +314,66 @@ class ExactGradient:
             ws.run_steps(min(self.seg, n - m * self.seg), self.seis, None, self.nrec)
         return self.seis[:, :, self.rcv]
 
+    def _static(self):
+        """Static device buffers of one reverse step: the state before the step, the adjoints,
+        the gradient accumulators, the forcing row and the flow."""
+        if getattr(self, "_s", None) is None:
+            ops, dev = self.ops, self.ws.dev
+            sa, sz, sw = ((ops.nb, 4, ops.nz, ops.nx), (ops.nb, 2, ops.nzpml, ops.nx), (ops.nb, 2, ops.nz, ops.nhx))
+            z = lambda sh: torch.zeros(sh, dtype=F64, device=dev)  # noqa: E731
+            self._s = dict(a=z(sa), Pz=z(sz), Px=z(sw), la=z(sa), lZ=z(sz), lW=z(sw), gx=z((ops.nz, ops.nx)),
+                           gz=z((ops.nz, ops.nx)), f=z((ops.nb, ops.nx)), v0x=z((ops.nz, ops.nx)),
+                           v0z=z((ops.nz, ops.nx)))
+        return self._s
+
+    def _reverse_step(self):
+        """Recompute the stages of one step from the static state and apply the transposed step
+        to the static adjoints in place, accumulating the flow gradient."""
+        S, ops = self._s, self.ops
+        _, _, _, caches = ops.step(S["a"], S["Pz"], S["Px"], S["v0x"], S["v0z"], S["f"])
+        la, lZ, lW, g1, g2 = ops.step_T(S["la"], S["lZ"], S["lW"], S["v0x"], S["v0z"], caches)
+        S["la"].copy_(la)
+        S["lZ"].copy_(lZ)
+        S["lW"].copy_(lW)
+        S["gx"].add_(g1)
+        S["gz"].add_(g2)
+
+    def _run_reverse_step(self):
+        """One reverse step, replayed from a CUDA graph when capture works (the same launches
+        on the same buffers), eagerly otherwise."""
+        if self.use_graph and self._graph is None:
+            S = self._s
+            keep = {k: v.clone() for k, v in S.items()}
+            try:
+                side = torch.cuda.Stream(device=self.ws.dev)
+                side.wait_stream(torch.cuda.current_stream(self.ws.dev))
+                with torch.cuda.stream(side):
+                    for _ in range(2):
+                        self._reverse_step()
+                torch.cuda.current_stream(self.ws.dev).wait_stream(side)
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    self._reverse_step()
+                self._graph = g
+            except RuntimeError:
+                self.use_graph = False
+            for k, v in keep.items():  # the warm-up and capture ran on the live buffers
+                S[k].copy_(v)
+        if self._graph is not None:
+            self._graph.replay()
+        else:
+            self._reverse_step()
+
     def gradient(self, psi: torch.Tensor, grad_rec: torch.Tensor) -> torch.Tensor:
         """dL/dpsi for dL/d(records at the receivers) = grad_rec (nb, nrec, nrcv), at the psi of
         the last forward call."""
         ws, ops, run = self.ws, self.ops, self.run
-        v0x, v0z = ws.bg["v0x"][0], ws.bg["v0z"][0]
         so, n = run.steps_out, run.nsteps
-        la = torch.zeros((ops.nb, 4, ops.nz, ops.nx), dtype=F64, device=ws.dev)
-        lZ = torch.zeros((ops.nb, 2, ops.nzpml, ops.nx), dtype=F64, device=ws.dev)
-        lW = torch.zeros((ops.nb, 2, ops.nz, ops.nhx), dtype=F64, device=ws.dev)
-        gx = torch.zeros((ops.nz, ops.nx), dtype=F64, device=ws.dev)
-        gz = torch.zeros_like(gx)
+        S = self._static()
+        for k in ("la", "lZ", "lW", "gx", "gz"):
+            S[k].zero_()
+        S["v0x"].copy_(ws.bg["v0x"][0])
+        S["v0z"].copy_(ws.bg["v0z"][0])
         grad_rec = grad_rec.to(device=ws.dev, dtype=F64)
         for m in range(self.nseg - 1, -1, -1):
             n0, n1 = m * self.seg, min((m + 1) * self.seg, n)
@@ -335,13 +383,16 @@ class ExactGradient:
                 ws.run_steps(1, None, None, 0)
             for step in range(n1 - 1, n0 - 1, -1):
                 if step % so == 0 and step // so < self.nrec:  # record taken after this step
-                    la[:, 3, ops.k_obs, self.rcv] += grad_rec[:, step // so, :]
-                a, Pz, Px = self._views(self.segbuf[step - n0])
-                _, _, _, caches = ops.step(a, Pz, Px, v0x, v0z, self._forcing(step))
-                la, lZ, lW, g1, g2 = ops.step_T(la, lZ, lW, v0x, v0z, caches)
-                gx += g1
-                gz += g2
-        return self.psi_gradient(gx, gz)
+                    S["la"][:, 3, ops.k_obs, self.rcv] += grad_rec[:, step // so, :]
+                for dst, src in zip((S["a"], S["Pz"], S["Px"]), self._views(self.segbuf[step - n0])):
+                    dst.copy_(src)
+                fc = self._forcing(step)
+                if fc is None:
+                    S["f"].zero_()
+                else:
+                    S["f"].copy_(fc)
+                self._run_reverse_step()
+        return self.psi_gradient(S["gx"].clone(), S["gz"].clone())
 
     def psi_gradient(self, gx: torch.Tensor, gz: torch.Tensor) -> torch.Tensor:
         """Transpose of psi -> (v0x, v0z) = (-d_z(rho0 c psi / R) / rho0, d_x(rho0 c psi / R) / rho0)

@@ -116,6 +116,11 @@ def test_gradient_matches_central_differences():
     loss = 0.5 * ((records(psi, eg) - data) ** 2).sum()
     loss.backward()
     g = psi.grad.detach().clone()
+    assert eg._graph is not None  # the reverse step ran from its CUDA graph
+    eager = ExactGradient(ws, rcv, segment=40, use_graph=False)
+    eager.forward(psi.detach())
+    ge = eager.gradient(psi.detach(), records(psi.detach(), eg) - data)
+    assert torch.allclose(ge, g, rtol=1e-12, atol=0.0)
     env = pt.abs() / pt.abs().max()
     dirs = [pt, torch.roll(pt, 9, dims=1), env * _rand(tuple(pt.shape), 21),
             env * torch.sin(torch.arange(pt.shape[1], device="cuda", dtype=F64) * 0.3)[None, :] * pt.abs().max()]
