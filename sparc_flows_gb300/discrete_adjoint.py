@@ -26,6 +26,8 @@ time, and applies the transposed stages in reverse order:
 The flow enters through the advection terms -2 v0x d_x v - 2 v0z d_z v of each stage; their
 derivative with respect to v0 is accumulated from the recomputed stage inputs, and v0 =
 curl(rho0 c psi) / rho0 (driver.f90:94-115) is linear in psi, so its transpose gives dL/dpsi.
+The sound speed enters through p = -c^2 rho0 div - ...: dL/d(c^2 rho0) = -sum lambda_p div over
+stages and steps (the exact counterpart of kernel_c, with the PML profiles held fixed).
 Pointwise algebra runs as device tensor arithmetic; every derivative, transposed derivative and
 transposed filter is one of the plan's kernels.
 """
@@ -146,7 +148,7 @@ class StepOperators:
         """Right-hand side of one stage (physics2d.f90:943-1094) for the stage input X (nb, 4, nz,
         nx) = (xi_x, xi_z, v_x, v_z) and PML auxiliaries Pz (nb, 2, nzpml, nx) = (psi_vz, psi_p),
         Px (nb, 2, nz, 2 npmlhor) = (psi_vx, psi_gradp_x).  forcing (nb, nx) is added to RHS v_z at
-        the injection row.  Returns (R, RPz, RPx, the four velocity derivatives)."""
+        the injection row.  Returns (R, RPz, RPx, the four velocity derivatives and div)."""
         xi_x, xi_z, v_x, v_z = X.unbind(1)
         pr, xc = self.prow, self.xcol
         dxx = self.dx(xi_x)
@@ -169,7 +171,7 @@ class StepOperators:
         Rvz = -self.rhoinv * (gpz + rho * self.g)
         if forcing is not None:
             Rvz[:, self.k_inj, :] += forcing
-        d = (self.dx(v_x), self.dz(v_x, 1), self.dx(v_z), self.dz(v_z, 1))
+        d = (self.dx(v_x), self.dz(v_x, 1), self.dx(v_z), self.dz(v_z, 1), div)
         Rvx = Rvx - 2.0 * v0x * d[0] - 2.0 * v0z * d[1]
         Rvz = Rvz - 2.0 * v0x * d[2] - 2.0 * v0z * d[3]
         R = self._zero_boundaries(torch.stack((v_x.clone(), v_z.clone(), Rvx, Rvz), 1))
@@ -177,7 +179,8 @@ class StepOperators:
 
     def rhs_T(self, lR, lRPz, lRPx, v0x, v0z, d):
         """Transpose of the linear part of rhs: adjoints of (R, RPz, RPx) -> adjoints of (X, Pz,
-        Px), and the derivative of <lR, R> with respect to v0x, v0z (summed over the batch)."""
+        Px), and the derivatives of <lR, R> with respect to v0x, v0z and c2rho0 (summed over the
+        batch; d holds the stage's velocity derivatives and div, zeros for the operator alone)."""
         pr, xc = self.prow, self.xcol
         lR = self._zero_boundaries(lR.clone())
         lRxx, lRxz, lRvx, lRvz = lR.unbind(1)
@@ -198,7 +201,8 @@ class StepOperators:
         lgpx[:, :, xc] = lgpx[:, :, xc] + self.ax * lRPx[:, 1]
         lpsig = lgpx[:, :, xc] + self.bx * lRPx[:, 1]
         lp = lp + self.dxT(lgpx)
-        # pressure
+        # pressure p = -c2rho0 div - gradp0_z xi_z
+        gc2 = (-(lp * d[4])).sum(0) if len(d) > 4 else torch.zeros_like(gv0x)
         ldiv = ldiv - self.c2rho0 * lp
         lxiz = lxiz - self.gp0 * lp
         # x-PML of dxi_x/dx
@@ -214,7 +218,7 @@ class StepOperators:
         ldxx[:, -1, :] = ldxx[:, -1, :] - self.ut * lpre
         lxix = self.dxT(ldxx)
         lX = torch.stack((lxix, lxiz, lvx, lvz), 1)
-        return lX, torch.stack((lpsivz, lpsip), 1), torch.stack((lpsivx, lpsig), 1), gv0x, gv0z
+        return lX, torch.stack((lpsivz, lpsip), 1), torch.stack((lpsivx, lpsig), 1), gv0x, gv0z, gc2
 
     # ---- one step -------------------------------------------------------------------------
     def filt(self, a):
@@ -239,23 +243,25 @@ class StepOperators:
 
     def step_T(self, la, lPz, lPx, v0x, v0z, caches):
         """Transpose of step (linear part) given the adjoints of its outputs; returns the adjoints
-        of its inputs and the gradient with respect to v0x, v0z."""
+        of its inputs and the gradients with respect to v0x, v0z and c2rho0."""
         mu = self.filtT(la)
         lA, lZ0, lW0 = mu.clone(), lPz.clone(), lPx.clone()
         lR, lRPz, lRPx = self.dt * mu, self.dt * lPz, self.dt * lPx
         gx = torch.zeros((self.nz, self.nx), dtype=F64, device=la.device)
         gz = torch.zeros_like(gx)
+        gc = torch.zeros_like(gx)
         for s in range(4, -1, -1):
-            lX, lZ, lW, g1, g2 = self.rhs_T(lR, lRPz, lRPx, v0x, v0z, caches[s])
+            lX, lZ, lW, g1, g2, g3 = self.rhs_T(lR, lRPz, lRPx, v0x, v0z, caches[s])
             gx += g1
             gz += g2
+            gc += g3
             lA += lX
             lZ0 += lZ
             lW0 += lW
             if s > 0:
                 b = self.betas[s]
                 lR, lRPz, lRPx = b * lX, b * lZ, b * lW
-        return lA, lZ0, lW0, gx, gz
+        return lA, lZ0, lW0, gx, gz, gc
 
 
 class ExactGradient:
@@ -322,7 +328,8 @@ class ExactGradient:
             sa, sz, sw = ((ops.nb, 4, ops.nz, ops.nx), (ops.nb, 2, ops.nzpml, ops.nx), (ops.nb, 2, ops.nz, ops.nhx))
             z = lambda sh: torch.zeros(sh, dtype=F64, device=dev)  # noqa: E731
             self._s = dict(a=z(sa), Pz=z(sz), Px=z(sw), la=z(sa), lZ=z(sz), lW=z(sw), gx=z((ops.nz, ops.nx)),
-                           gz=z((ops.nz, ops.nx)), f=z((ops.nb, ops.nx)), v0x=z((ops.nz, ops.nx)),
+                           gz=z((ops.nz, ops.nx)), gc=z((ops.nz, ops.nx)), f=z((ops.nb, ops.nx)),
+                           v0x=z((ops.nz, ops.nx)),
                            v0z=z((ops.nz, ops.nx)))
         return self._s
 
@@ -331,12 +338,13 @@ class ExactGradient:
         to the static adjoints in place, accumulating the flow gradient."""
         S, ops = self._s, self.ops
         _, _, _, caches = ops.step(S["a"], S["Pz"], S["Px"], S["v0x"], S["v0z"], S["f"])
-        la, lZ, lW, g1, g2 = ops.step_T(S["la"], S["lZ"], S["lW"], S["v0x"], S["v0z"], caches)
+        la, lZ, lW, g1, g2, g3 = ops.step_T(S["la"], S["lZ"], S["lW"], S["v0x"], S["v0z"], caches)
         S["la"].copy_(la)
         S["lZ"].copy_(lZ)
         S["lW"].copy_(lW)
         S["gx"].add_(g1)
         S["gz"].add_(g2)
+        S["gc"].add_(g3)
 
     def _run_reverse_step(self):
         """One reverse step, replayed from a CUDA graph when capture works (the same launches
@@ -370,7 +378,7 @@ class ExactGradient:
         ws, ops, run = self.ws, self.ops, self.run
         so, n = run.steps_out, run.nsteps
         S = self._static()
-        for k in ("la", "lZ", "lW", "gx", "gz"):
+        for k in ("la", "lZ", "lW", "gx", "gz", "gc"):
             S[k].zero_()
         S["v0x"].copy_(ws.bg["v0x"][0])
         S["v0z"].copy_(ws.bg["v0z"][0])
@@ -392,7 +400,18 @@ class ExactGradient:
                 else:
                     S["f"].copy_(fc)
                 self._run_reverse_step()
-        return self.psi_gradient(S["gx"].clone(), S["gz"].clone())
+        self.last = {"v0x": S["gx"].clone(), "v0z": S["gz"].clone(), "c2rho0": S["gc"].clone()}
+        return self.psi_gradient(self.last["v0x"], self.last["v0z"])
+
+    def set_c2rho0(self, c2rho0: torch.Tensor):
+        """Replace the plan's c^2 rho0 field (nz, nx), the PML profiles kept: the parameter whose
+        gradient ``last["c2rho0"]`` is (needs a plan built with a sound-speed field, cmul)."""
+        ws = self.ws
+        if ws.bg["c2rho0"].dim() != 3:
+            raise ValueError("the plan has a depth-only c^2 rho0; build it with cmul")
+        # in place: the operators (and a captured reverse-step graph) hold this buffer's address
+        ws.bg["c2rho0"].copy_(c2rho0.to(device=ws.dev, dtype=F64).reshape(1, self.ops.nz, self.ops.nx))
+        ws._upload_background()
 
     def psi_gradient(self, gx: torch.Tensor, gz: torch.Tensor) -> torch.Tensor:
         """Transpose of psi -> (v0x, v0z) = (-d_z(rho0 c psi / R) / rho0, d_x(rho0 c psi / R) / rho0)

@@ -47,7 +47,7 @@ def test_stage_transpose_dot_product():
     X, Z, W = _rand(sa, 1), _rand(sz, 2), _rand(sw, 3)
     lR, lZ, lW = _rand(sa, 4), _rand(sz, 5), _rand(sw, 6)
     R, RZ, RW, _ = ops.rhs(X, Z, W, v0x, v0z)
-    tX, tZ, tW, _, _ = ops.rhs_T(lR, lZ, lW, v0x, v0z, [torch.zeros_like(X[:, 0])] * 4)
+    tX, tZ, tW = ops.rhs_T(lR, lZ, lW, v0x, v0z, [torch.zeros_like(X[:, 0])] * 4)[:3]
     lhs = _dot((lR, lZ, lW), (R, RZ, RW))
     rhs = _dot((tX, tZ, tW), (X, Z, W))
     ws.close()
@@ -136,3 +136,42 @@ def test_gradient_matches_central_differences():
     assert float(loss.detach()) > 0
     for r in ratios:
         assert abs(r - 1.0) < 1e-7, ratios
+
+
+def test_sound_speed_gradient_matches_central_differences():
+    """dL/d(c^2 rho0) (PML profiles fixed) against central differences along three directions:
+    data from the plan with a 5 % sound-speed bump, gradient at the unperturbed field."""
+    from sparc_flows_gb300.discrete_adjoint import ExactGradient, records
+    from sparc_flows_gb300.solver import WaveSolver
+    run = RunConfig(nx=128, nz=300, xlength_cm=200e8, nsteps=150, flows=True)
+    model = M.polytrope(300)
+    psi = torch.as_tensor(M.gaussian_psi(run, model, M.psi_amplitude_for_peak(run, model, 240.0)), device="cuda")
+    ws = WaveSolver(run, model, nbatch=2, precision=64, psi=psi.cpu().numpy(), cmul=M.c_bump(run, model))
+    ws.set_forward_sources([M.SourceSpec(-20.0), M.SourceSpec(25.0)])
+    rcv = receiver_columns(run, n=32, x0=-62.0, dx=4.0)
+    eg = ExactGradient(ws, rcv, segment=40)
+    c_true = ws.bg["c2rho0"][0].clone()
+    with torch.no_grad():
+        data = records(psi, eg).clone()
+    nz, nx = c_true.shape
+    base = c_true[:, :1].expand(nz, nx).contiguous()  # the depth profile without the bump
+    eg.set_c2rho0(base)
+    rec = eg.forward(psi)
+    eg.gradient(psi, rec - data)
+    g = eg.last["c2rho0"]
+    zc = torch.arange(nz, device="cuda", dtype=F64)[:, None]
+    env = torch.exp(-((zc - 200.0) / 40.0) ** 2) * torch.ones((1, nx), device="cuda", dtype=F64)
+    dev = {}
+    for seed in (31, 32, 33):
+        d = env * base * _rand((nz, nx), seed)
+        for eps in (1e-4, 1e-5):
+            lp_ = []
+            for sgn in (1.0, -1.0):
+                eg.set_c2rho0(base + sgn * eps * d)
+                lp_.append(0.5 * float(((eg.forward(psi) - data) ** 2).sum()))
+            dev[(seed, eps)] = (lp_[0] - lp_[1]) / (2 * eps) / float((g * d).sum()) - 1.0
+    ws.close()
+    for seed in (31, 32, 33):
+        # central-difference truncation is O(eps^2): 10x smaller steps, ~100x smaller deviation
+        assert abs(dev[(seed, 1e-5)]) < 1e-7, dev
+        assert abs(dev[(seed, 1e-5)]) < 0.05 * abs(dev[(seed, 1e-4)]) + 1e-9, dev
