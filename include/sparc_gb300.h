@@ -279,9 +279,11 @@ int sparc3d_set_state(sparc3d_plan_t *plan, const void *src, void *stream);
 
 /* ---------------------------------------------------------------------------------------------
  * 2-D velocity-pressure-density solver: option 5, MP_QUIET_SPONGE_2D (physics2d.f90:1099-1137,
- * a sponge layer, USE_PML off) or option 6, MP_QUIET_PML_2D (physics2d.f90:662-713, the
- * vertical PML), the RK of STEP and FILTER_VARS_2D on the five fields.  Fields [nz][nbatch][nx]; the state is five of
- * them: rho, v_x, v_y (zero), v_z, p (initialize.f90:500-504).
+ * a sponge layer, USE_PML off), option 6, MP_QUIET_PML_2D (physics2d.f90:662-713, the
+ * vertical PML) or option 12, MP_MHD_PML_2d (physics2d.f90:411-474 with the magnetic part of
+ * PML_BOUNDARY_ACCOUNTING_2D, 1162-1200), the RK of STEP and FILTER_VARS_2D on every field.
+ * Fields [nz][nbatch][nx]; the state is five of them: rho, v_x, v_y (zero), v_z, p
+ * (initialize.f90:500-504), and for option 12 eight: b_x, b_y (zero), b_z follow.
  * ------------------------------------------------------------------------------------------- */
 typedef struct sparc5_plan sparc5_plan_t;
 
@@ -293,15 +295,19 @@ typedef struct {
     double betas[5];
     int steps_out, k_src, k_obs;    /* record cadence, 0-based e_rad, o_rad */
     int option;                     /* 5: MP_QUIET_SPONGE_2D (physics2d.f90:1099-1137);
-                                       6: MP_QUIET_PML_2D (physics2d.f90:662-713) */
-    int npmlbot, npmltop;           /* vertical PML levels (option 6) */
+                                       6: MP_QUIET_PML_2D (physics2d.f90:662-713);
+                                       12: MP_MHD_PML_2d (physics2d.f90:411-474) */
+    int npmlbot, npmltop;           /* vertical PML levels (options 6 and 12) */
 } sparc5_config_t;
 
 /* FP64 device profiles [nz]: stretch, rhoinv, rho0, c2rho0, gradp0_z, gradrho0_z, g (no PML
  * decay), source_dep, sponge (spongez, physics2d.f90:62-69). */
 typedef struct {
     const double *stretch, *rhoinv, *rho0, *c2rho0, *gradp0_z, *gradrho0_z, *g, *source_dep, *sponge;
-    const double *az, *bz;  /* [npmlbot + npmltop] (physics2d.f90:288-332), option 6 */
+    const double *az, *bz;  /* [npmlbot + npmltop] (physics2d.f90:288-332), options 6 and 12 */
+    const double *box, *boz; /* option 12: background field [nz][nx], B / dimb (initialize.f90:759);
+                                curlboy = d box/dz - d boz/dx is formed on the device
+                                (physics2d.f90:166-168) */
 } sparc5_background_t;
 
 int sparc5_plan_create(const sparc5_config_t *cfg, sparc5_plan_t **plan);
@@ -314,7 +320,7 @@ int sparc5_reset_state(sparc5_plan_t *plan, int time0, void *stream);
 /* nsteps steps; v_z at k_obs ([nbatch][nx]) appended to seis after each step whose index is a
  * multiple of steps_out. */
 int sparc5_forward(sparc5_plan_t *plan, int nsteps, void *seis, int nrec_cap, int *nrec, void *stream);
-/* [5][nz][nbatch][nx] of the plan precision (device). */
+/* [nf][nz][nbatch][nx] of the plan precision (device): nf = 5, or 8 for option 12. */
 int sparc5_get_state(sparc5_plan_t *plan, void *dst, void *stream);
 
 /* ---------------------------------------------------------------------------------------------

@@ -33,6 +33,7 @@ def _lib():
         L.orc5_get_int.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
         L.orc5_get_profile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _dp]
         L.orc5_get_profile.restype = ctypes.c_long
+        L.orc5_set_magnetic.argtypes = [ctypes.c_void_p, _dp, _dp]
         _bound = True
     return L
 
@@ -42,8 +43,8 @@ def _p(a):
 
 
 class SimSponge:
-    """One 2-D option-5 (sponge) or option-6 (PML) solve on the CPU; state (5, nz, nx): rho,
-    v_x, v_y, v_z, p."""
+    """One 2-D option-5 (sponge), option-6 (PML) or option-12 (MHD with PML) solve on the CPU;
+    state (5, nz, nx): rho, v_x, v_y, v_z, p, and for option 12 (8, nz, nx) with b_x, b_y, b_z."""
 
     def __init__(self, nx, model, xlength_cm, timestep=2.0, excitdep_cm=-150e5, obsheight_cm=200e5, npmlhor=9,
                  steps_out=15, filter_all_x=False, option=5, npmlbot=10, npmltop=10):
@@ -55,6 +56,14 @@ class SimSponge:
         self.h = self.L.orc5_create(ctypes.byref(p), _p(m))
         if not self.h:
             raise ValueError("orc5_create failed")
+        self.nf = self.L.orc5_get_int(self.h, b"nf")
+
+    def set_magnetic(self, box, boz):
+        """Background field (nz, nx), nondimensional (B / dimb); option 12 only."""
+        bx = np.ascontiguousarray(box, dtype=np.float64)
+        bz = np.ascontiguousarray(boz, dtype=np.float64)
+        if self.L.orc5_set_magnetic(self.h, _p(bx), _p(bz)) != 0:
+            raise ValueError("set_magnetic needs option 12")
 
     def set_source(self, pattern, amp):
         pt = np.ascontiguousarray(pattern, dtype=np.float64)
@@ -67,7 +76,7 @@ class SimSponge:
         return seis[:n]
 
     def state(self):
-        a = np.zeros((5, self.nz, self.nx))
+        a = np.zeros((self.nf, self.nz, self.nx))
         self.L.orc5_get_state(self.h, _p(a))
         return a
 

@@ -1,10 +1,16 @@
 /* sparc_oracle_sponge.c -- CPU FP64 oracle of the 2-D sponge step (test infrastructure).
  *
  * A plain-C restatement of the reference's option 5, MP_QUIET_SPONGE_2D: the velocity-pressure-
- * density formulation with a sponge layer instead of a PML, and of option 6, MP_QUIET_PML_2D
- * (the same formulation with the vertical PML, physics2d.f90:662-713, 1142-1160, 288-332), used
- * only by the tests as the checker of the GPU path (csrc/sparc_sponge.cu).  Fields are [nz][nx], x fastest; the state is
- * five of them: rho, v_x, v_y (zero in 2-D), v_z, p (initialize.f90:500-512).
+ * density formulation with a sponge layer instead of a PML, of option 6, MP_QUIET_PML_2D
+ * (the same formulation with the vertical PML, physics2d.f90:662-713, 1142-1160, 288-332), and
+ * of option 12, MP_MHD_PML_2d (physics2d.f90:411-474 with the magnetic part of
+ * PML_BOUNDARY_ACCOUNTING_2D, 1162-1200), used only by the tests as the checker of the GPU path
+ * (csrc/sparc_sponge.cu).  Fields are [nz][nx], x fastest; the state is five of them: rho, v_x,
+ * v_y (zero in 2-D), v_z, p (initialize.f90:500-512), and for option 12 eight: b_x, b_y (zero in
+ * 2-D), b_z follow.  Option 12's background field (box, boz) is given; curlboy = d box/dz -
+ * d boz/dx as physics2d.f90:166-168 (the reduction factor there ends as 1).  The background
+ * stratification stays laterally uniform (gradrho0_x = gradp0_x = 0: a current-free field needs
+ * no change of it).
  *
  * Followed lines:
  *   grid, stretch, solar_data, betas  as sparc_oracle.c (initialize.f90:195-226, 466-474,
@@ -40,7 +46,7 @@ typedef struct {
     double xlength, timestep, excitdep, obsheight;
     int steps_out;
     int filter_all_x; /* 1: every column (HORIZONTAL_PMLS off) */
-    int option;       /* 5: MP_QUIET_SPONGE_2D; 6: MP_QUIET_PML_2D (USE_PML, no sponge) */
+    int option;       /* 5: MP_QUIET_SPONGE_2D; 6: MP_QUIET_PML_2D (USE_PML, no sponge); 12: MP_MHD_PML_2d */
     int npmlbot, npmltop;
 } orc5_params;
 
@@ -57,8 +63,11 @@ typedef struct {
     double *pattern, *amp;
     int namp, time;
     int nzpml;
-    double *az, *bz;                    /* [nz], option 6 */
-    double *pmlvars, *psipml, *scrpml;  /* [2][nzpml][nx]: psi_p, psi_vz */
+    double *az, *bz;                    /* [nz], options 6 and 12 */
+    double *pmlvars, *psipml, *scrpml;  /* [npa][nzpml][nx]: psi_p, psi_vz (+ psi of dz flux2, dz b_x) */
+    int nf, npa;                        /* fields of the state, PML auxiliaries */
+    double *box, *boz, *curlboy;        /* [nz][nx], option 12 */
+    double *flux, *dzbx, *dzf, *dxf, *dxbz;
 } orc5_sim;
 
 static double *z5(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
@@ -109,7 +118,11 @@ orc5_sim *orc5_create(const orc5_params *prm, const double *model)
     s->z = z5(nz); s->stretch = z5(nz); s->g = z5(nz); s->rho0 = z5(nz); s->p0 = z5(nz); s->c2 = z5(nz);
     s->rhoinv = z5(nz); s->c2rho0 = z5(nz); s->gradrho0_z = z5(nz); s->gradp0_z = z5(nz); s->sponge = z5(nz);
     s->source_dep = z5(nz);
-    s->a = z5(5 * N); s->temp = z5(5 * N); s->scr = z5(5 * N);
+    s->nf = prm->option == 12 ? 8 : 5;
+    s->npa = prm->option == 12 ? 4 : (prm->option == 6 ? 2 : 0);
+    s->a = z5(s->nf * N); s->temp = z5(s->nf * N); s->scr = z5(s->nf * N);
+    s->box = z5(N); s->boz = z5(N); s->curlboy = z5(N);
+    s->flux = z5(N); s->dzbx = z5(N); s->dzf = z5(N); s->dxf = z5(N); s->dxbz = z5(N);
     s->dvxdx = z5(N); s->dvzdz = z5(N); s->gpx = z5(N); s->gpz = z5(N); s->tmp = z5(N);
     s->pattern = z5(nx);
     const double dimc = 1e6, dimrho = 1e-3, diml = ORC5_RSUN;
@@ -156,11 +169,11 @@ orc5_sim *orc5_create(const orc5_params *prm, const double *model)
         s->gradrho0_z[k] *= s->stretch[k];
         s->gradp0_z[k] *= s->stretch[k];
     }
-    s->nzpml = prm->option == 6 ? prm->npmlbot + prm->npmltop : 0;
+    s->nzpml = (prm->option == 6 || prm->option == 12) ? prm->npmlbot + prm->npmltop : 0;
     s->az = z5(nz); s->bz = z5(nz);
-    s->pmlvars = z5(2 * (size_t)s->nzpml * nx); s->psipml = z5(2 * (size_t)s->nzpml * nx);
-    s->scrpml = z5(2 * (size_t)s->nzpml * nx);
-    if (prm->option == 6) {
+    s->pmlvars = z5((size_t)s->npa * s->nzpml * nx); s->psipml = z5((size_t)s->npa * s->nzpml * nx);
+    s->scrpml = z5((size_t)s->npa * s->nzpml * nx);
+    if (prm->option == 6 || prm->option == 12) {
         /* USE_PML: no sponge (physics2d.f90:289-290) and the vertical PML of physics2d.f90:288-332
          * (laterally uniform background; the top layer's damping takes c at level nz-5) */
         const int nb = prm->npmlbot, nt = prm->npmltop;
@@ -242,13 +255,104 @@ static void orc6_rhs(orc5_sim *s)
     }
 }
 
+/* The background field of option 12 (nondimensional, B / dimb, initialize.f90:759): box, boz
+ * [nz][nx] and curlboy = d box/dz - d boz/dx (physics2d.f90:166-168). */
+int orc5_set_magnetic(orc5_sim *s, const double *box, const double *boz)
+{
+    if (s->p.option != 12) return -1;
+    memcpy(s->box, box, s->N * sizeof(double));
+    memcpy(s->boz, boz, s->N * sizeof(double));
+    d5_z(s, s->box, s->curlboy, 1);
+    d5_x(s, s->boz, s->tmp);
+    for (size_t q = 0; q < s->N; q++) s->curlboy[q] -= s->tmp[q];
+    return 0;
+}
+
+/* MP_MHD_PML_2d (physics2d.f90:411-474) with PML_BOUNDARY_ACCOUNTING_2D (1142-1200): the
+ * non-magnetic accounting of psi_p, psi_vz, then the two-point smoothing of dv_z/dz on the PML
+ * rows 2..npmlbot and nz-npmltop+1..nz-1 (1-based) and the PML of d flux2/dz and d b_x/dz. */
+static void orc12_rhs(orc5_sim *s)
+{
+    const int nx = s->nx, nz = s->nz, nb = s->p.npmlbot, nt = s->p.npmltop;
+    const size_t N = s->N, P = (size_t)s->nzpml * nx;
+    const double *rho = s->temp, *vx = s->temp + N, *vz = s->temp + 3 * N, *p = s->temp + 4 * N;
+    const double *bx = s->temp + 5 * N, *bz = s->temp + 7 * N;
+    double *sc = s->scr;
+    for (size_t q = 0; q < N; q++) s->flux[q] = -(vx[q] * s->boz[q] - vz[q] * s->box[q]);
+    d5_z(s, vz, s->dvzdz, 1);
+    d5_z(s, p, s->gpz, 1);
+    d5_z(s, bx, s->dzbx, 1);
+    d5_z(s, s->flux, s->dzf, 1);
+    for (int k = 0; k < nz; k++) {
+        const int pi = pml5(s, k);
+        if (pi < 0) continue;
+        for (int i = 0; i < nx; i++) {
+            const size_t q = (size_t)k * nx + i, m = (size_t)pi * nx + i;
+            s->scrpml[m] = s->az[k] * s->gpz[q] + s->bz[k] * s->psipml[m];
+            s->gpz[q] = s->gpz[q] + s->psipml[m];
+            s->scrpml[P + m] = s->az[k] * s->dvzdz[q] + s->bz[k] * s->psipml[P + m];
+            s->dvzdz[q] = s->dvzdz[q] + s->psipml[P + m];
+        }
+    }
+    double *t = s->tmp;
+    for (int k = 1; k <= nb - 1; k++)
+        for (int i = 0; i < nx; i++)
+            t[(size_t)k * nx + i] = 0.5 * (s->dvzdz[(size_t)(k - 1) * nx + i] + s->dvzdz[(size_t)(k + 1) * nx + i]);
+    for (int k = nz - nt; k <= nz - 2; k++)
+        for (int i = 0; i < nx; i++)
+            t[(size_t)k * nx + i] = 0.5 * (s->dvzdz[(size_t)(k - 1) * nx + i] + s->dvzdz[(size_t)(k + 1) * nx + i]);
+    for (int k = 1; k <= nb - 1; k++) memcpy(s->dvzdz + (size_t)k * nx, t + (size_t)k * nx, nx * sizeof(double));
+    for (int k = nz - nt; k <= nz - 2; k++) memcpy(s->dvzdz + (size_t)k * nx, t + (size_t)k * nx, nx * sizeof(double));
+    for (int k = 0; k < nz; k++) {
+        const int pi = pml5(s, k);
+        if (pi < 0) continue;
+        for (int i = 0; i < nx; i++) {
+            const size_t q = (size_t)k * nx + i, m = (size_t)pi * nx + i;
+            s->scrpml[2 * P + m] = s->az[k] * s->dzf[q] + s->bz[k] * s->psipml[2 * P + m];
+            s->dzf[q] = s->dzf[q] + s->psipml[2 * P + m];
+            s->scrpml[3 * P + m] = s->az[k] * s->dzbx[q] + s->bz[k] * s->psipml[3 * P + m];
+            s->dzbx[q] = s->dzbx[q] + s->psipml[3 * P + m];
+        }
+    }
+    d5_x(s, vx, s->dvxdx);
+    d5_x(s, p, s->gpx);
+    d5_x(s, s->flux, s->dxf);
+    d5_x(s, bz, s->dxbz);
+    const double amp = s->time < s->namp ? s->amp[s->time] : 0.0;
+    for (int k = 0; k < nz; k++)
+        for (int i = 0; i < nx; i++) {
+            const size_t q = (size_t)k * nx + i;
+            const double div = s->dvxdx[q] + s->dvzdz[q];
+            const double cur = s->dzbx[q] - s->dxbz[q];
+            const double t1 = s->boz[q] * cur + bz[q] * s->curlboy[q];
+            const double t3 = -s->box[q] * cur - bx[q] * s->curlboy[q];
+            sc[q] = -s->gradrho0_z[k] * vz[q] - s->rho0[k] * div;
+            sc[N + q] = s->rhoinv[k] * (t1 - s->gpx[q]);
+            sc[2 * N + q] = 0.0;
+            double r = s->rhoinv[k] * (t3 - s->gpz[q]);
+            r = r - s->rhoinv[k] * rho[q] * s->g[k];
+            if (abs(k - s->e_rad) <= 4) r = r + (s->pattern[i] * amp) * s->source_dep[k];
+            sc[3 * N + q] = r;
+            sc[4 * N + q] = -s->c2rho0[k] * div - vz[q] * s->gradp0_z[k];
+            sc[5 * N + q] = -s->dzf[q];
+            sc[6 * N + q] = 0.0;
+            sc[7 * N + q] = s->dxf[q];
+        }
+    for (int l = 0; l < 8; l++)
+        for (int i = 0; i < nx; i++) {
+            sc[(size_t)l * N + i] = 0.0;
+            sc[(size_t)l * N + (size_t)(nz - 1) * nx + i] = 0.0;
+        }
+}
+
 void orc5_destroy(orc5_sim *s)
 {
     if (!s) return;
     double *ptrs[] = {s->fre, s->fim, s->ftr, s->fti, s->z, s->stretch, s->g, s->rho0, s->p0, s->c2, s->rhoinv,
                       s->c2rho0, s->gradrho0_z, s->gradp0_z, s->sponge, s->source_dep, s->a, s->temp, s->scr,
                       s->dvxdx, s->dvzdz, s->gpx, s->gpz, s->tmp, s->pattern, s->amp, s->az, s->bz,
-                      s->pmlvars, s->psipml, s->scrpml};
+                      s->pmlvars, s->psipml, s->scrpml, s->box, s->boz, s->curlboy, s->flux, s->dzbx,
+                      s->dzf, s->dxf, s->dxbz};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
     orc_fft_delete(s->fx);
     free(s);
@@ -305,7 +409,7 @@ static void orc5_filter(orc5_sim *s)
     const int nx = s->nx, nz = s->nz, nh = s->p.npmlhor;
     double *temp = s->tmp;
     const int i0 = s->p.filter_all_x ? 0 : nh - 1, i1 = s->p.filter_all_x ? nx - 1 : nx - nh;
-    for (int l = 0; l < 5; l++) {
+    for (int l = 0; l < s->nf; l++) {
         double *a = s->a + (size_t)l * s->N;
 #define A5(k, i) a[(size_t)(k) * nx + (i)]
 #define T5(k, i) temp[(size_t)(k) * nx + (i)]
@@ -325,7 +429,7 @@ static void orc5_filter(orc5_sim *s)
 
 void orc5_step(orc5_sim *s)
 {
-    const size_t N5 = 5 * s->N, P2 = 2 * (size_t)s->nzpml * s->nx;
+    const size_t N5 = (size_t)s->nf * s->N, P2 = (size_t)s->npa * s->nzpml * s->nx;
     for (int rk = 0; rk < 5; rk++) {
         if (rk == 0) {
             memcpy(s->temp, s->a, N5 * sizeof(double));
@@ -334,7 +438,8 @@ void orc5_step(orc5_sim *s)
             for (size_t q = 0; q < N5; q++) s->temp[q] = s->a[q] + s->betas[rk] * s->scr[q];
             for (size_t q = 0; q < P2; q++) s->psipml[q] = s->pmlvars[q] + s->betas[rk] * s->scrpml[q];
         }
-        if (s->p.option == 6) orc6_rhs(s);
+        if (s->p.option == 12) orc12_rhs(s);
+        else if (s->p.option == 6) orc6_rhs(s);
         else orc5_rhs(s);
     }
     for (size_t q = 0; q < N5; q++) s->a[q] = s->a[q] + s->deltat * s->scr[q];
@@ -358,7 +463,7 @@ int orc5_run(orc5_sim *s, int nsteps, double *seis)
 
 int orc5_get_state(const orc5_sim *s, double *a)
 {
-    memcpy(a, s->a, 5 * s->N * sizeof(double));
+    memcpy(a, s->a, (size_t)s->nf * s->N * sizeof(double));
     return 0;
 }
 
@@ -366,6 +471,7 @@ int orc5_get_int(const orc5_sim *s, const char *name)
 {
     if (!strcmp(name, "e_rad")) return s->e_rad;
     if (!strcmp(name, "o_rad")) return s->o_rad;
+    if (!strcmp(name, "nf")) return s->nf;
     return -1;
 }
 

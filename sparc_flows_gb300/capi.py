@@ -109,7 +109,7 @@ class Sparc5Background(ctypes.Structure):
     """sparc5_background_t (device pointers)."""
 
     _fields_ = [(n, _vp) for n in ("stretch", "rhoinv", "rho0", "c2rho0", "gradp0_z", "gradrho0_z", "g",
-                                    "source_dep", "sponge", "az", "bz")]
+                                    "source_dep", "sponge", "az", "bz", "box", "boz")]
 
 
 class Sparc3DBackground(ctypes.Structure):

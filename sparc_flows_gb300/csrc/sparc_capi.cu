@@ -1745,7 +1745,9 @@ struct Plan5 {
     std::vector<void *> allocs;
     T *A = nullptr, *SCR = nullptr, *X = nullptr, *DVX = nullptr, *DVZ = nullptr, *GX = nullptr, *GZ = nullptr;
     T *prof = nullptr, *pat = nullptr;
-    T *PV = nullptr, *SPV = nullptr, *PSI = nullptr;  // option 6: psi_p, psi_vz [2][npml][nb][nx]
+    T *PV = nullptr, *SPV = nullptr, *PSI = nullptr;  // PML auxiliaries [npa][npml][nb][nx] (options 6, 12)
+    T *FLUX = nullptr, *DZBX = nullptr, *DZF = nullptr, *DXF = nullptr, *DXBZ = nullptr;  // option 12 work
+    T *MAG = nullptr;                                  // option 12: box, boz, curlboy [3][nz][nx]
     DevZ<T> z1;
     DevFFT<T> fx;
     S5Bg<T> bg{};
@@ -1775,17 +1777,24 @@ Plan5<float> &plan5<float>(sparc5_plan *p) { return p->s32; }
 template <>
 Plan5<double> &plan5<double>(sparc5_plan *p) { return p->s64; }
 
+// Fields of the state, PML auxiliaries and PML levels of an option.
+int nf5(const sparc5_config_t &c) { return c.option == 12 ? 8 : 5; }
+int npa5(const sparc5_config_t &c) { return c.option == 12 ? 4 : (c.option == 6 ? 2 : 0); }
+int npml5(const sparc5_config_t &c) { return (c.option == 6 || c.option == 12) ? c.npmlbot + c.npmltop : 0; }
+
 template <typename T>
 int alloc_plan5(sparc5_plan *p)
 {
     Plan5<T> &S = plan5<T>(p);
     const sparc5_config_t &c = p->cfg;
-    const size_t F = (size_t)p->F, nz = c.nz, npml = c.option == 6 ? c.npmlbot + c.npmltop : 0;
-    const size_t P2 = 2 * npml * c.nbatch * c.nx;
+    const size_t F = (size_t)p->F, nz = c.nz, npml = npml5(c), nf = nf5(c);
+    const size_t P2 = (size_t)npa5(c) * npml * c.nbatch * c.nx;
+    const size_t FM = c.option == 12 ? F : 0, NM = c.option == 12 ? 3 * nz * (size_t)c.nx : 0;
     struct Req { T **ptr; size_t n; };
-    std::vector<Req> reqs = {{&S.A, 5 * F}, {&S.SCR, 5 * F}, {&S.X, 5 * F}, {&S.DVX, F}, {&S.DVZ, F}, {&S.GX, F},
+    std::vector<Req> reqs = {{&S.A, nf * F}, {&S.SCR, nf * F}, {&S.X, nf * F}, {&S.DVX, F}, {&S.DVZ, F}, {&S.GX, F},
                              {&S.GZ, F}, {&S.prof, 9 * nz + 2 * npml}, {&S.pat, (size_t)c.nbatch * c.nx},
-                             {&S.PV, P2}, {&S.SPV, P2}, {&S.PSI, P2}};
+                             {&S.PV, P2}, {&S.SPV, P2}, {&S.PSI, P2}, {&S.FLUX, FM}, {&S.DZBX, FM}, {&S.DZF, FM},
+                             {&S.DXF, FM}, {&S.DXBZ, FM}, {&S.MAG, NM}};
     for (auto &r : reqs) {
         void *ptr = nullptr;
         const size_t bytes = std::max<size_t>(r.n, 1) * sizeof(T);
@@ -1811,6 +1820,11 @@ int alloc_plan5(sparc5_plan *p)
     S.bg.sponge = q; q += nz;
     S.bg.az = q; q += npml;
     S.bg.bz = q;
+    if (c.option == 12) {
+        S.bg.box = S.MAG;
+        S.bg.boz = S.MAG + nz * c.nx;
+        S.bg.curl = S.MAG + 2 * nz * c.nx;
+    }
     return SPARC_OK;
 }
 
@@ -1821,16 +1835,18 @@ cudaError_t step5(sparc5_plan *p, T *seis, int cap, int &nrec, cudaStream_t st)
     Plan5<T> &S = plan5<T>(p);
     const sparc5_config_t &c = p->cfg;
     const long long F = p->F, lvl = (long long)c.nbatch * c.nx;
-    const bool pml = c.option == 6;
+    const bool pml = c.option == 6 || c.option == 12, mhd = c.option == 12;
+    const int nf = nf5(c);
     const S5Args a{c.nx, c.nz, c.nbatch, c.k_src, c.filter_all_x ? 0 : c.npmlhor - 1,
-                   c.filter_all_x ? c.nx - 1 : c.nx - c.npmlhor, pml ? c.npmlbot : 0, pml ? c.npmltop : 0};
-    const long long P2 = pml ? 2LL * (c.npmlbot + c.npmltop) * lvl : 0;
+                   c.filter_all_x ? c.nx - 1 : c.nx - c.npmlhor, pml ? c.npmlbot : 0, pml ? c.npmltop : 0,
+                   nf, npa5(c)};
+    const long long P2 = (long long)npa5(c) * npml5(c) * lvl;
     const T amp = (T)(p->time >= 0 && p->time < (int)p->amp.size() ? p->amp[p->time] : 0.0);
     cudaError_t e;
     for (int s = 0; s < 5; s++) {
         const T *X = S.A, *PSI = S.PV;
         if (s > 0) {
-            e = launch_s3_stage_in<T>(5 * F, S.A, S.SCR, S.X, (T)c.betas[s], P2, S.PV, S.SPV, S.PSI, st);
+            e = launch_s3_stage_in<T>(nf * F, S.A, S.SCR, S.X, (T)c.betas[s], P2, S.PV, S.SPV, S.PSI, st);
             if (e != cudaSuccess) return e;
             X = S.X;
             PSI = S.PSI;
@@ -1840,9 +1856,18 @@ cudaError_t step5(sparc5_plan *p, T *seis, int cap, int &nrec, cudaStream_t st)
         if (e == cudaSuccess) e = launch_ddx<T>(X + 4 * F, S.GX, nrows, c.nx, (T)c.stretchx, S.fx.twr, S.fx.twi, S.fx.kap, st);
         if (e == cudaSuccess) e = launch_ddz<T>(S.z1.tab, p->nch, p->L, X + 3 * F, S.DVZ, (int)lvl, c.nz, nullptr, S.stretch, 0, st);
         if (e == cudaSuccess) e = launch_ddz<T>(S.z1.tab, p->nch, p->L, X + 4 * F, S.GZ, (int)lvl, c.nz, nullptr, S.stretch, 0, st);
+        if (e == cudaSuccess && mhd) {  // flux, d flux/dx, d flux/dz, d b_z/dx, d b_x/dz
+            e = launch_s12_flux<T>(a, S.bg, X, S.FLUX, st);
+            if (e == cudaSuccess) e = launch_ddx<T>(S.FLUX, S.DXF, nrows, c.nx, (T)c.stretchx, S.fx.twr, S.fx.twi, S.fx.kap, st);
+            if (e == cudaSuccess) e = launch_ddx<T>(X + 7 * F, S.DXBZ, nrows, c.nx, (T)c.stretchx, S.fx.twr, S.fx.twi, S.fx.kap, st);
+            if (e == cudaSuccess) e = launch_ddz<T>(S.z1.tab, p->nch, p->L, S.FLUX, S.DZF, (int)lvl, c.nz, nullptr, S.stretch, 0, st);
+            if (e == cudaSuccess) e = launch_ddz<T>(S.z1.tab, p->nch, p->L, X + 5 * F, S.DZBX, (int)lvl, c.nz, nullptr, S.stretch, 0, st);
+        }
         if (e == cudaSuccess)
-            e = pml ? launch_s6_rhs<T>(a, S.bg, X, S.SCR, S.DVX, S.DVZ, S.GX, S.GZ, PSI, S.SPV, S.pat, amp, st)
-                    : launch_s5_rhs<T>(a, S.bg, X, S.SCR, S.DVX, S.DVZ, S.GX, S.GZ, S.pat, amp, st);
+            e = mhd ? launch_s12_rhs<T>(a, S.bg, X, S.SCR, S.DVX, S.DVZ, S.GX, S.GZ, S.DZBX, S.DZF, S.DXF, S.DXBZ, PSI,
+                                        S.SPV, S.pat, amp, st)
+                : pml ? launch_s6_rhs<T>(a, S.bg, X, S.SCR, S.DVX, S.DVZ, S.GX, S.GZ, PSI, S.SPV, S.pat, amp, st)
+                      : launch_s5_rhs<T>(a, S.bg, X, S.SCR, S.DVX, S.DVZ, S.GX, S.GZ, S.pat, amp, st);
         if (e != cudaSuccess) return e;
     }
     e = launch_s5_end<T>(a, S.A, S.SCR, (T)c.deltat, pml ? S.PV : nullptr, S.SPV, st);
@@ -1867,10 +1892,20 @@ int set_bg5(sparc5_plan *p, const sparc5_background_t *bg, cudaStream_t st)
     const double *prof[9] = {bg->stretch, bg->rhoinv, bg->rho0, bg->c2rho0, bg->gradp0_z, bg->gradrho0_z, bg->g,
                              bg->source_dep, bg->sponge};
     for (int i = 0; i < 9; i++) CK(cast_to<T>(prof[i], S.prof + (size_t)i * nz, nz, st));
-    if (p->cfg.option == 6) {
+    if (p->cfg.option == 6 || p->cfg.option == 12) {
         const int npml = p->cfg.npmlbot + p->cfg.npmltop;
         CK(cast_to<T>(bg->az, S.prof + (size_t)9 * nz, npml, st));
         CK(cast_to<T>(bg->bz, S.prof + (size_t)9 * nz + npml, npml, st));
+    }
+    if (p->cfg.option == 12) {  // box, boz; curlboy = d box/dz - d boz/dx (physics2d.f90:166-168)
+        const int nx = p->cfg.nx;
+        const size_t NM = (size_t)nz * nx;
+        T *box = S.MAG, *boz = S.MAG + NM, *curl = S.MAG + 2 * NM;
+        CK(cast_to<T>(bg->box, box, NM, st));
+        CK(cast_to<T>(bg->boz, boz, NM, st));
+        CK(launch_ddz<T>(S.z1.tab, p->nch, p->L, box, curl, nx, nz, nullptr, S.stretch, 0, st));
+        CK(launch_ddx<T>(boz, S.DXBZ, nz, nx, (T)p->cfg.stretchx, S.fx.twr, S.fx.twi, S.fx.kap, st));
+        CK(launch_s5_axpy<T>((long long)NM, curl, S.DXBZ, T(-1), st));
     }
     return SPARC_OK;
 }
@@ -1889,9 +1924,9 @@ int sparc5_plan_create(const sparc5_config_t *cfg, sparc5_plan_t **out)
         cfg->k_obs >= cfg->nz || (!cfg->filter_all_x && (cfg->npmlhor < 1 || 2 * cfg->npmlhor > cfg->nx)) ||
         (long long)cfg->nz * cfg->nbatch > 2147483647LL)
         return fail(SPARC_ERR_SIZE, "sparc5_plan_create: bad grid, batch or rows");
-    if ((cfg->option != 5 && cfg->option != 6) ||
-        (cfg->option == 6 && (cfg->npmlbot < 1 || cfg->npmltop < 1 || cfg->npmlbot + cfg->npmltop >= cfg->nz)))
-        return fail(SPARC_ERR_ARG, "sparc5_plan_create: option must be 5 or 6 (with PML levels for 6)");
+    if ((cfg->option != 5 && cfg->option != 6 && cfg->option != 12) ||
+        (cfg->option != 5 && (cfg->npmlbot < 1 || cfg->npmltop < 1 || cfg->npmlbot + cfg->npmltop >= cfg->nz)))
+        return fail(SPARC_ERR_ARG, "sparc5_plan_create: option must be 5, 6 or 12 (with PML levels for 6 and 12)");
     sparc5_plan *p = new sparc5_plan();
     p->cfg = *cfg;
     p->F = (long long)cfg->nx * cfg->nbatch * cfg->nz;
@@ -1925,7 +1960,9 @@ int sparc5_set_background(sparc5_plan_t *p, const sparc5_background_t *bg, void 
                              bg->source_dep, bg->sponge};
     for (const double *q : need)
         if (!q) return fail(SPARC_ERR_ARG, "sparc5_set_background: missing profile");
-    if (p->cfg.option == 6 && (!bg->az || !bg->bz)) return fail(SPARC_ERR_ARG, "sparc5_set_background: PML az, bz missing");
+    if (p->cfg.option != 5 && (!bg->az || !bg->bz)) return fail(SPARC_ERR_ARG, "sparc5_set_background: PML az, bz missing");
+    if (p->cfg.option == 12 && (!bg->box || !bg->boz))
+        return fail(SPARC_ERR_ARG, "sparc5_set_background: option 12 needs the background field box, boz");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int rc = p->cfg.precision == 32 ? set_bg5<float>(p, bg, st) : set_bg5<double>(p, bg, st);
     if (rc == SPARC_OK) p->have_bg = true;
@@ -1950,10 +1987,10 @@ int sparc5_reset_state(sparc5_plan_t *p, int time0, void *stream)
     const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
     void *A = p->cfg.precision == 32 ? (void *)p->s32.A : (void *)p->s64.A;
     void *SCR = p->cfg.precision == 32 ? (void *)p->s32.SCR : (void *)p->s64.SCR;
-    CK(cudaMemsetAsync(A, 0, 5 * p->F * es, st));
-    CK(cudaMemsetAsync(SCR, 0, 5 * p->F * es, st));
-    if (p->cfg.option == 6) {
-        const size_t P2 = 2 * (size_t)(p->cfg.npmlbot + p->cfg.npmltop) * p->cfg.nbatch * p->cfg.nx;
+    CK(cudaMemsetAsync(A, 0, nf5(p->cfg) * p->F * es, st));
+    CK(cudaMemsetAsync(SCR, 0, nf5(p->cfg) * p->F * es, st));
+    if (npa5(p->cfg) > 0) {
+        const size_t P2 = (size_t)npa5(p->cfg) * npml5(p->cfg) * p->cfg.nbatch * p->cfg.nx;
         void *PV = p->cfg.precision == 32 ? (void *)p->s32.PV : (void *)p->s64.PV;
         void *SPV = p->cfg.precision == 32 ? (void *)p->s32.SPV : (void *)p->s64.SPV;
         CK(cudaMemsetAsync(PV, 0, P2 * es, st));
@@ -1983,7 +2020,7 @@ int sparc5_get_state(sparc5_plan_t *p, void *dst, void *stream)
     if (!p || !dst) return fail(SPARC_ERR_ARG, "sparc5_get_state: null argument");
     const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
     const void *A = p->cfg.precision == 32 ? (const void *)p->s32.A : (const void *)p->s64.A;
-    CK(cudaMemcpyAsync(dst, A, 5 * p->F * es, cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
+    CK(cudaMemcpyAsync(dst, A, nf5(p->cfg) * p->F * es, cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
     return SPARC_OK;
 }
 

@@ -439,11 +439,13 @@ cudaError_t launch_s3_end(const S3Args &a, T *A, const T *SCR, T dt, int filter,
 // 2-D sponge step (option 5, sparc_sponge.cu).  Fields [nz][nb][nx].
 struct S5Args {
     int nx, nz, nb, e_rad, i0, i1;  // filter columns [i0, i1]
-    int npmlbot, npmltop;           // option 6
+    int npmlbot, npmltop;           // options 6 and 12
+    int nf, npa;                    // fields of the state (5 or 8), PML auxiliaries (0, 2 or 4)
 };
 template <typename T>
-struct S5Bg {  // profiles in z; az, bz [npmlbot + npmltop] (option 6)
+struct S5Bg {  // profiles in z; az, bz [npmlbot + npmltop] (options 6, 12)
     const T *rhoinv, *rho0, *c2rho0, *gradp0_z, *gradrho0_z, *g, *source_dep, *sponge, *az, *bz;
+    const T *box, *boz, *curl;  // option 12: background field and curlboy, [nz][nx]
 };
 template <typename T>
 cudaError_t launch_s5_rhs(const S5Args &a, const S5Bg<T> &bg, const T *X, T *SCR, const T *DVX, const T *DVZ,
@@ -453,6 +455,14 @@ cudaError_t launch_s6_rhs(const S5Args &a, const S5Bg<T> &bg, const T *X, T *SCR
                           const T *GX, const T *GZ, const T *PSI, T *SPSI, const T *PAT, T amp, cudaStream_t st);
 template <typename T>
 cudaError_t launch_s5_end(const S5Args &a, T *A, const T *SCR, T dt, T *PV, const T *SPV, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s12_flux(const S5Args &a, const S5Bg<T> &bg, const T *X, T *FLUX, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s12_rhs(const S5Args &a, const S5Bg<T> &bg, const T *X, T *SCR, const T *DVX, const T *DVZ,
+                           const T *GX, const T *GZ, const T *DZBX, const T *DZF, const T *DXF, const T *DXBZ,
+                           const T *PSI, T *SPSI, const T *PAT, T amp, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s5_axpy(long long n, T *Y, const T *X, T a, cudaStream_t st);
 
 template <int CW, int R>
 cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st);

@@ -12,7 +12,7 @@ import math
 
 import numpy as np
 
-from .config import DIMC, RSUN_CM, RunConfig
+from .config import DIMC, DIMRHO, RSUN_CM, RunConfig
 
 NUPEAK = float(np.float32(0.0017))   # params.i:66, single-precision literal
 NUWIDTH = float(np.float32(0.0055))
@@ -128,6 +128,22 @@ class SourceSpec:
     sigma: float = 0.5                # Mm, Gaussian profile
     temporal: int = TEMPORAL_RICKER
     nu0: float = 0.003                # Hz, Ricker peak frequency
+
+
+DIMB = (4.0 * np.pi * DIMC ** 2 * DIMRHO) ** 0.5  # magnetic unit, initialize.f90:759
+
+
+def potential_field(nx: int, model: np.ndarray, xlength_cm: float, b_gauss: float, m: int = 1):
+    """A current-free background field for the 2-D MHD step: B = curl(A y) with
+    A = (B0 / k) cos(k X) exp(k (z - 1)), k = 2 pi m R / xlength, X the horizontal coordinate and z
+    the radius in solar radii, B0 = b_gauss at z = 1; box = -dA/dz, boz = dA/dX as the reference
+    forms them from a flux function (physics2d.f90:124-134).  Its curl vanishes, so it needs no
+    change of the hydrostatic stratification.  Returns (box, boz), (nz, nx), in units of dimb."""
+    X = np.arange(nx) / nx * xlength_cm / RSUN_CM
+    k = 2.0 * np.pi * m * RSUN_CM / xlength_cm
+    e = np.exp(k * (model[:, 0] - 1.0))[:, None]
+    b0 = b_gauss / DIMB
+    return -b0 * np.cos(k * X)[None, :] * e, -b0 * np.sin(k * X)[None, :] * e
 
 
 def source_profile(run: RunConfig, spec: SourceSpec) -> np.ndarray:

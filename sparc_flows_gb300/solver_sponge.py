@@ -1,5 +1,6 @@
 """2-D velocity-pressure-density solver: option 5 (MP_QUIET_SPONGE_2D, a sponge absorber,
-physics2d.f90:1099-1137) or option 6 (MP_QUIET_PML_2D, the vertical PML, physics2d.f90:662-713);
+physics2d.f90:1099-1137), option 6 (MP_QUIET_PML_2D, the vertical PML, physics2d.f90:662-713) or
+option 12 (MP_MHD_PML_2d, the same with a background magnetic field, physics2d.f90:411-474);
 the Python host of the sparc5_* C ABI (csrc/sparc_sponge.cu, csrc/sparc_capi.cu).
 
 Set-up as the reference's mp_Initialize_RHS_2d (physics2d.f90:23-332): e_rad, o_rad,
@@ -7,7 +8,9 @@ source_dep, rhoinv, c2 rho0, the background gradients d rho0/dz, d p0/dz, and ei
 profile spongez (physics2d.f90:62-69; spongexyz = spongez for a periodic box) or, with USE_PML,
 no sponge (physics2d.f90:289-290) and the vertical PML coefficients with their decay of the
 background gradients and g (physics2d.f90:288-332).  State (5, nz, nbatch, nx): rho, v_x, v_y,
-v_z, p.
+v_z, p; for option 12 (8, nz, nbatch, nx) with b_x, b_y, b_z.  Option 12 takes the background
+field (box, boz), (nz, nx) in units of dimb = (4 pi dimc^2 dimrho)^(1/2) (initialize.f90:759);
+the stratification stays laterally uniform, as a current-free field leaves it.
 """
 from __future__ import annotations
 
@@ -26,7 +29,7 @@ class WaveSolverSponge:
     def __init__(self, nx: int, model: np.ndarray, xlength_cm: float, nbatch: int = 1, precision: int = 64,
                  timestep: float = 2.0, excitdep_cm: float = -150e5, obsheight_cm: float = 200e5, npmlhor: int = 9,
                  steps_out: int = 15, filter_all_x: bool = False, option: int = 5, npmlbot: int = 10,
-                 npmltop: int = 10, device="cuda"):
+                 npmltop: int = 10, box=None, boz=None, device="cuda"):
         self.L = capi.lib()
         self.nx, self.nz, self.nb = nx, model.shape[0], nbatch
         self.dtype = torch.float32 if precision == 32 else torch.float64
@@ -50,7 +53,7 @@ class WaveSolverSponge:
         nz = self.nz
         az = np.zeros(npmlbot + npmltop)
         bz = np.zeros(npmlbot + npmltop)
-        if option == 6:
+        if option in (6, 12):
             sponge = np.zeros(nz)
             l005 = f(0.005)
             for k in range(nz):
@@ -87,6 +90,12 @@ class WaveSolverSponge:
         h = ctypes.c_void_p()
         capi.check(self.L.sparc5_plan_create(ctypes.byref(cfg), ctypes.byref(h)), "sparc5_plan_create")
         self.plan = h
+        self.nf = 8 if option == 12 else 5
+        if option == 12:
+            if box is None or boz is None:
+                raise ValueError("option 12 needs the background field box, boz (nz, nx)")
+            self.profiles["box"] = np.ascontiguousarray(box, dtype=np.float64).reshape(nz, nx)
+            self.profiles["boz"] = np.ascontiguousarray(boz, dtype=np.float64).reshape(nz, nx)
         self._bg = {k: torch.as_tensor(v, dtype=torch.float64, device=self.dev) for k, v in self.profiles.items()}
         bg = capi.Sparc5Background()
         for k, t in self._bg.items():
@@ -118,7 +127,7 @@ class WaveSolverSponge:
         return seis[:n.value]
 
     def state(self) -> torch.Tensor:
-        st = torch.empty((5, self.nz, self.nb, self.nx), dtype=self.dtype, device=self.dev)
+        st = torch.empty((self.nf, self.nz, self.nb, self.nx), dtype=self.dtype, device=self.dev)
         capi.check(self.L.sparc5_get_state(self.plan, st.data_ptr(), self._stream()), "sparc5_get_state")
         return st
 
