@@ -8,7 +8,13 @@
 // a matrix-vector product per column with the transposed matrix.  FP64 throughout.
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "sparc_gb300.h"
+
+namespace sparc {
+int report_error(int code, const std::string &msg);
+}
 
 namespace {
 
@@ -48,9 +54,13 @@ __global__ void __launch_bounds__(CM_X *CM_Y) colmat_kernel(const double *__rest
 extern "C" int sparc_colmat_apply(const double *W, int nz, const double *in, double *out, int nb, int nx, int i0,
                                   int i1, int accumulate, void *stream)
 {
-    if (!W || !in || !out || nz < 1 || nb < 1 || nx < 1 || in == out) return SPARC_ERR_ARG;
-    if (nb > 65535 || (nz + CM_Y - 1) / CM_Y > 65535) return SPARC_ERR_ARG;
+    if (!W || !in || !out || nz < 1 || nb < 1 || nx < 1 || in == out)
+        return sparc::report_error(SPARC_ERR_ARG, "sparc_colmat_apply: null, empty or aliased argument");
+    if (nb > 65535 || (nz + CM_Y - 1) / CM_Y > 65535)
+        return sparc::report_error(SPARC_ERR_SIZE, "sparc_colmat_apply: grid too large");
     dim3 grid((nx + CM_X - 1) / CM_X, (nz + CM_Y - 1) / CM_Y, nb);
     colmat_kernel<<<grid, dim3(CM_X, CM_Y), 0, (cudaStream_t)stream>>>(W, nz, in, out, nx, i0, i1, accumulate);
-    return cudaGetLastError() == cudaSuccess ? SPARC_OK : SPARC_ERR_CUDA;
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? SPARC_OK
+                            : sparc::report_error(SPARC_ERR_CUDA, std::string("sparc_colmat_apply: ") + cudaGetErrorString(e));
 }

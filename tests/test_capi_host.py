@@ -45,6 +45,17 @@ def test_plan_create_rejects_bad_config_without_gpu_work():
     assert L.sparc_plan_create(None, ctypes.byref(h)) == -1
 
 
+def test_column_operator_rejects_bad_arguments_without_gpu_work():
+    """sparc_colmat_apply (the discrete adjoint's transposed column operators) validates before any
+    CUDA call: null or aliased buffers are SPARC_ERR_ARG with a message."""
+    L = capi.lib()
+    assert L.sparc_colmat_apply(None, 300, None, None, 1, 128, 0, 127, 0, None) == -1
+    assert b"sparc_colmat_apply" in L.sparc_last_error()
+    p = ctypes.c_void_p(4096)
+    assert L.sparc_colmat_apply(p, 300, p, p, 1, 128, 0, 127, 0, None) == -1  # in == out
+    assert b"aliased" in L.sparc_last_error()
+
+
 @pytest.mark.parametrize("ibc", [0, 1, 2, 3])
 @pytest.mark.parametrize("lmax", [16, 32])
 def test_partitioned_tables_match_dbyd2(ibc, lmax):
