@@ -139,6 +139,18 @@ def _forward(run, model, directory, contrib, jobno, src, precision, device, comp
     res = ws.forward(snapshots=keep)
     seis, snaps = (res if keep else (res, None))
     s = seis.double().cpu().numpy()[0]
+    _write_forward_files(out, run, s)
+    if keep:
+        _save_partial_states(out, snaps[0], run.steps_out, forward=True)
+    if not compute_data:
+        _adjoint_source_files(run, directory, contrib, jobno, xloc, s, device)
+    ws.close()
+    return 0
+
+
+def _write_forward_files(out, run, s):
+    """vz_cc.fits (records (nrec, 1, nx)), kernel_info, timeline and rms_hist of a forward run
+    (all_modules.f90:1081-1101, driver.f90:337-475)."""
     fits.write(os.path.join(out, "vz_cc.fits"), s[:, None, :])
     with open(os.path.join(out, "kernel_info"), "w") as f:
         f.write(f"{0}\n{run.nsteps - 1}\n")
@@ -147,19 +159,20 @@ def _forward(run, model, directory, contrib, jobno, src, precision, device, comp
             f.write(f"{i} {-run.solartime_h * 3600.0 + (i + 1) * run.timestep}\n")
     with open(os.path.join(out, "rms_hist"), "w") as f:
         f.write(f"{float(np.sqrt((s[-1] ** 2).sum()))}\n")
-    if keep:
-        _save_partial_states(out, snaps[0], run.steps_out, forward=True)
-    if not compute_data:
-        data_p = os.path.join(directory, "data", f"{contrib}.fits")
-        data = fits.read(data_p).reshape(s.shape) if os.path.exists(data_p) else np.zeros_like(s)
-        if os.environ.get("SPARC_ADJOINT_SOURCE", "tt") == "waveform":
-            adir = os.path.join(directory, f"adjoint_src{contrib}")
-            os.makedirs(adir, exist_ok=True)
-            fits.write(os.path.join(adir, "source.fits"), (s - data)[::-1][:, None, :])
-        else:
-            _tt_adjoint(run, directory, contrib, jobno, xloc, s, data, device)
-    ws.close()
-    return 0
+
+
+def _adjoint_source_files(run, directory, contrib, jobno, xloc, s, device):
+    """The adjoint source of a forward run that is not a data run, against <dir>/data/NN.fits:
+    the travel-time source and misfit files, or with SPARC_ADJOINT_SOURCE=waveform the
+    time-reversed waveform residual, written to adjoint_srcNN/source.fits."""
+    data_p = os.path.join(directory, "data", f"{contrib}.fits")
+    data = fits.read(data_p).reshape(s.shape) if os.path.exists(data_p) else np.zeros_like(s)
+    if os.environ.get("SPARC_ADJOINT_SOURCE", "tt") == "waveform":
+        adir = os.path.join(directory, f"adjoint_src{contrib}")
+        os.makedirs(adir, exist_ok=True)
+        fits.write(os.path.join(adir, "source.fits"), (s - data)[::-1][:, None, :])
+    else:
+        _tt_adjoint(run, directory, contrib, jobno, xloc, s, data, device)
 
 
 def _tt_adjoint(run, directory, contrib, jobno, xloc, synth, data, device):
@@ -198,10 +211,14 @@ def _adjoint(run, model, directory, contrib, jobno, precision, device):
     ws.set_adjoint_sources(vr[None])
     _, snaps = ws.forward(snapshots=True)
     _save_partial_states(adir, snaps[0], run.steps_out, forward=False)
-    with open(os.path.join(adir, "kernel_info"), "w") as f:
-        f.write(f"{run.forcing_length}\n{((run.nsteps - 1) // run.cadforcing_step) * run.cadforcing_step}\n")
+    _write_adjoint_info(adir, run)
     ws.close()
     return 0
+
+
+def _write_adjoint_info(adir, run):
+    with open(os.path.join(adir, "kernel_info"), "w") as f:
+        f.write(f"{run.forcing_length}\n{((run.nsteps - 1) // run.cadforcing_step) * run.cadforcing_step}\n")
 
 
 def _kernels(run, model, directory, contrib, jobno, precision, device):
@@ -219,16 +236,22 @@ def _kernels(run, model, directory, contrib, jobno, precision, device):
         ws.close()
         return 1
     ker = kernels_from_partial_states(ws, fsn, asn)
-    kdir = os.path.join(directory, "kernel")
-    os.makedirs(kdir, exist_ok=True)
-    for name in ("kernel_c", "kernel_vx", "kernel_vz", "kernel_psi", "hessian"):
-        fits.write(os.path.join(kdir, f"{name}_{contrib}.fits"), ker[name][:, None, :])
+    _write_kernel_files(directory, contrib, ker)
     for d in (fdir, adir):  # kernels.f90:593-595 removes the partial states
         for f in os.listdir(d):
             if f == "partial_states.npy" or f.endswith("_partial.fits"):
                 os.remove(os.path.join(d, f))
     ws.close()
     return 0
+
+
+def _write_kernel_files(directory, contrib, ker):
+    """kernel/{kernel_c, kernel_vx, kernel_vz, kernel_psi, hessian}_NN.fits, (nz, 1, nx) each
+    (kernels.f90:583-590)."""
+    kdir = os.path.join(directory, "kernel")
+    os.makedirs(kdir, exist_ok=True)
+    for name in ("kernel_c", "kernel_vx", "kernel_vz", "kernel_psi", "hessian"):
+        fits.write(os.path.join(kdir, f"{name}_{contrib}.fits"), ker[name][:, None, :])
 
 
 # partial-state fields of the reference's files (all_modules.f90:759-775) and their slot in the

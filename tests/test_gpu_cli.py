@@ -167,3 +167,40 @@ def test_unknown_source_fails_with_nonzero_status(tmp_path):
     shutil.copy(os.path.join(ROOT, "tests", "golden", "Spectral"), code / "Instruction_src05_ls00")
     r = run_sparc(code, "05", "00", dict(os.environ, SPARC_NSTEPS="16"))
     assert r.returncode != 0
+
+
+def test_batched_iteration_equals_per_source_runs(tmp_path, monkeypatch):
+    """full_batched (all sources in one FwdAdjKernels batch) writes the same records and kernel
+    files as the three sparc runs per source that full.py makes (full.py:18-59)."""
+    from sparc_flows_gb300 import cli, full_batched
+    from sparc_flows_gb300.config import RunConfig
+    code = tmp_path / "code"
+    data = tmp_path / "data_dir"
+    code.mkdir()
+    data.mkdir()
+    (code / "params.i").write_text(PARAMS.format(dir=str(data)))
+    np.savetxt(code / "polytrope_gen", M.polytrope(300), fmt="%.17e")
+    (data / "master.pixels").write_text("-10.0\n15.0\n")
+    run = RunConfig(nx=128, nz=300, xlength_cm=200e8, nsteps=46)
+    fits.write(str(data / "model_psi_ls00.fits"), M.gaussian_psi(run, M.polytrope(300), 0.05)[:, None, :])
+    monkeypatch.chdir(code)
+    for k, v in dict(SPARC_NSTEPS="46", SPARC_PRECISION="64", SPARC_ADJOINT_SOURCE="waveform").items():
+        monkeypatch.setenv(k, v)
+    names = ("kernel_c", "kernel_vx", "kernel_vz", "kernel_psi", "hessian")
+    for nn in ("01", "02"):  # forward, adjoint, kernel stage per source
+        for instr in ("Spectral", "Adjoint", None):
+            if instr:
+                shutil.copy(os.path.join(ROOT, "tests", "golden", instr), code / f"Instruction_src{nn}_ls00")
+            assert cli.main([nn, "00"]) == 0
+            if instr == "Adjoint":
+                os.remove(code / f"Instruction_src{nn}_ls00")
+    per = {(nn, n): fits.read(str(data / "kernel" / f"{n}_{nn}.fits")) for nn in ("01", "02") for n in names}
+    vz = {nn: fits.read(str(data / f"forward_src{nn}_ls00" / "vz_cc.fits")) for nn in ("01", "02")}
+    shutil.rmtree(data / "kernel")
+    assert full_batched.main([]) == 0
+    for nn in ("01", "02"):
+        assert np.array_equal(fits.read(str(data / f"forward_src{nn}_ls00" / "vz_cc.fits")), vz[nn])
+        for n in names:
+            got = fits.read(str(data / "kernel" / f"{n}_{nn}.fits"))
+            assert np.abs(per[(nn, n)]).max() > 0
+            assert np.allclose(got, per[(nn, n)], rtol=1e-12, atol=1e-12 * np.abs(per[(nn, n)]).max()), (nn, n)
