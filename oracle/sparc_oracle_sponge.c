@@ -4,8 +4,9 @@
  * density formulation with a sponge layer instead of a PML, of option 6, MP_QUIET_PML_2D
  * (the same formulation with the vertical PML, physics2d.f90:662-713, 1142-1160, 288-332), and
  * of option 12, MP_MHD_PML_2d (physics2d.f90:411-474 with the magnetic part of
- * PML_BOUNDARY_ACCOUNTING_2D, 1162-1200), used only by the tests as the checker of the GPU path
- * (csrc/sparc_sponge.cu).  Fields are [nz][nx], x fastest; the state is five of them: rho, v_x,
+ * PML_BOUNDARY_ACCOUNTING_2D, 1162-1200), and of option 11, MP_MHD_SPONGE_2D (physics2d.f90:
+ * 588-658), used only by the tests as the checker of the GPU path (csrc/sparc_sponge.cu; option
+ * 11 has no GPU plan yet).  Fields are [nz][nx], x fastest; the state is five of them: rho, v_x,
  * v_y (zero in 2-D), v_z, p (initialize.f90:500-512), and for option 12 eight: b_x, b_y (zero in
  * 2-D), b_z follow.  Option 12's background field (box, boz) is given; curlboy = d box/dz -
  * d boz/dx as physics2d.f90:166-168 (the reduction factor there ends as 1).  The background
@@ -46,7 +47,8 @@ typedef struct {
     double xlength, timestep, excitdep, obsheight;
     int steps_out;
     int filter_all_x; /* 1: every column (HORIZONTAL_PMLS off) */
-    int option;       /* 5: MP_QUIET_SPONGE_2D; 6: MP_QUIET_PML_2D (USE_PML, no sponge); 12: MP_MHD_PML_2d */
+    int option;       /* 5: MP_QUIET_SPONGE_2D; 6: MP_QUIET_PML_2D (USE_PML, no sponge); 11: MP_MHD_SPONGE_2D;
+                         12: MP_MHD_PML_2d */
     int npmlbot, npmltop;
 } orc5_params;
 
@@ -118,7 +120,7 @@ orc5_sim *orc5_create(const orc5_params *prm, const double *model)
     s->z = z5(nz); s->stretch = z5(nz); s->g = z5(nz); s->rho0 = z5(nz); s->p0 = z5(nz); s->c2 = z5(nz);
     s->rhoinv = z5(nz); s->c2rho0 = z5(nz); s->gradrho0_z = z5(nz); s->gradp0_z = z5(nz); s->sponge = z5(nz);
     s->source_dep = z5(nz);
-    s->nf = prm->option == 12 ? 8 : 5;
+    s->nf = (prm->option == 11 || prm->option == 12) ? 8 : 5;
     s->npa = prm->option == 12 ? 4 : (prm->option == 6 ? 2 : 0);
     s->a = z5(s->nf * N); s->temp = z5(s->nf * N); s->scr = z5(s->nf * N);
     s->box = z5(N); s->boz = z5(N); s->curlboy = z5(N);
@@ -259,7 +261,7 @@ static void orc6_rhs(orc5_sim *s)
  * [nz][nx] and curlboy = d box/dz - d boz/dx (physics2d.f90:166-168). */
 int orc5_set_magnetic(orc5_sim *s, const double *box, const double *boz)
 {
-    if (s->p.option != 12) return -1;
+    if (s->p.option != 11 && s->p.option != 12) return -1;
     memcpy(s->box, box, s->N * sizeof(double));
     memcpy(s->boz, boz, s->N * sizeof(double));
     d5_z(s, s->box, s->curlboy, 1);
@@ -334,6 +336,61 @@ static void orc12_rhs(orc5_sim *s)
             if (abs(k - s->e_rad) <= 4) r = r + (s->pattern[i] * amp) * s->source_dep[k];
             sc[3 * N + q] = r;
             sc[4 * N + q] = -s->c2rho0[k] * div - vz[q] * s->gradp0_z[k];
+            sc[5 * N + q] = -s->dzf[q];
+            sc[6 * N + q] = 0.0;
+            sc[7 * N + q] = s->dxf[q];
+        }
+    for (int l = 0; l < 8; l++)
+        for (int i = 0; i < nx; i++) {
+            sc[(size_t)l * N + i] = 0.0;
+            sc[(size_t)l * N + (size_t)(nz - 1) * nx + i] = 0.0;
+        }
+}
+
+/* MP_MHD_SPONGE_2D (physics2d.f90:588-658): the sponge formulation with the background field;
+ * d p/dz with both boundary rows set by the caller (ibc 4, dbyd2.f:129-140): row 1
+ * (-c rho0 dv_z/dz - rho g) unstretch, row nz (c rho0 dv_z/dz - rho g) unstretch
+ * (physics2d.f90:605-611, c the sound speed, not its square; unstretch = 1 / stretch); d b_x/dz
+ * with ibc 0. */
+static void orc11_rhs(orc5_sim *s)
+{
+    const int nx = s->nx, nz = s->nz;
+    const size_t N = s->N;
+    const double *rho = s->temp, *vx = s->temp + N, *vz = s->temp + 3 * N, *p = s->temp + 4 * N;
+    const double *bx = s->temp + 5 * N, *bz = s->temp + 7 * N;
+    double *sc = s->scr;
+    d5_x(s, vx, s->dvxdx);
+    d5_z(s, vz, s->dvzdz, 1);
+    d5_x(s, p, s->gpx);
+    for (int i = 0; i < nx; i++) {
+        const size_t t0 = i, t1 = (size_t)(nz - 1) * nx + i;
+        s->gpz[t0] = (-sqrt(s->c2[0]) * s->rho0[0] * s->dvzdz[t0] - rho[t0] * s->g[0]) / s->stretch[0];
+        s->gpz[t1] = (sqrt(s->c2[nz - 1]) * s->rho0[nz - 1] * s->dvzdz[t1] - rho[t1] * s->g[nz - 1]) /
+                     s->stretch[nz - 1];
+    }
+    d5_z(s, p, s->gpz, 4);
+    d5_x(s, bz, s->dxbz);
+    d5_z(s, bx, s->dzbx, 0);
+    for (size_t q = 0; q < N; q++) s->flux[q] = -(vx[q] * s->boz[q] - vz[q] * s->box[q]);
+    d5_z(s, s->flux, s->dzf, 1);
+    d5_x(s, s->flux, s->dxf);
+    const double amp = s->time < s->namp ? s->amp[s->time] : 0.0;
+    for (int k = 0; k < nz; k++)
+        for (int i = 0; i < nx; i++) {
+            const size_t q = (size_t)k * nx + i;
+            const double sp = s->sponge[k];
+            const double div = s->dvxdx[q] + s->dvzdz[q];
+            const double cur = s->dzbx[q] - s->dxbz[q];
+            const double t1 = s->boz[q] * cur + bz[q] * s->curlboy[q];
+            const double t3 = -s->box[q] * cur - bx[q] * s->curlboy[q];
+            sc[q] = -s->gradrho0_z[k] * vz[q] - s->rho0[k] * div - sp * rho[q];
+            sc[N + q] = s->rhoinv[k] * (t1 - s->gpx[q]) - sp * vx[q];
+            sc[2 * N + q] = 0.0;
+            double r = s->rhoinv[k] * (t3 - s->gpz[q]) - sp * vz[q];
+            r = r - s->rhoinv[k] * rho[q] * s->g[k];
+            if (abs(k - s->e_rad) <= 4) r = r + (s->pattern[i] * amp) * s->source_dep[k];
+            sc[3 * N + q] = r;
+            sc[4 * N + q] = -s->c2rho0[k] * div - vz[q] * s->gradp0_z[k] - sp * p[q];
             sc[5 * N + q] = -s->dzf[q];
             sc[6 * N + q] = 0.0;
             sc[7 * N + q] = s->dxf[q];
@@ -439,6 +496,7 @@ void orc5_step(orc5_sim *s)
             for (size_t q = 0; q < P2; q++) s->psipml[q] = s->pmlvars[q] + s->betas[rk] * s->scrpml[q];
         }
         if (s->p.option == 12) orc12_rhs(s);
+        else if (s->p.option == 11) orc11_rhs(s);
         else if (s->p.option == 6) orc6_rhs(s);
         else orc5_rhs(s);
     }
