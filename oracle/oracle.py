@@ -56,6 +56,7 @@ def lib():
         L.orc_destroy.argtypes = [ctypes.c_void_p]
         L.orc_set_psi.argtypes = [ctypes.c_void_p, _c_double_p]
         L.orc_set_flow.argtypes = [ctypes.c_void_p, _c_double_p, _c_double_p]
+        L.orc_set_magnetic.argtypes = [ctypes.c_void_p, _c_double_p, _c_double_p]
         L.orc_set_forward_source.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
                                              ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int]
         L.orc_set_adjoint_source.argtypes = [ctypes.c_void_p, _c_double_p, ctypes.c_int, ctypes.c_int]
@@ -123,6 +124,14 @@ class OracleSim:
         a = np.ascontiguousarray(v0x, dtype=np.float64)
         b = np.ascontiguousarray(v0z, dtype=np.float64)
         self.L.orc_set_flow(self.h, _p(a), _p(b))
+
+    def set_magnetic(self, box, boz):
+        """Option 18 (MP_MHD_PML_2D_DISPL): background field (nz, nx) in units of dimb; the run must
+        have no flow."""
+        a = np.ascontiguousarray(box, dtype=np.float64)
+        b = np.ascontiguousarray(boz, dtype=np.float64)
+        if self.L.orc_set_magnetic(self.h, _p(a), _p(b)) != 0:
+            raise ValueError("orc_set_magnetic: the run has flows")
 
     def set_forward_source(self, xloc, spatial_kind=0, sigma=0.5, temporal_kind=0, nu0=0.003, nt=None):
         nt = nt if nt is not None else self.run.nsteps + 8

@@ -301,6 +301,11 @@ typedef struct orc_sim {
     double *forcing;   /* nx, adjoint Lagrange result, physics.f90:678-737 */
     int num_steps;     /* driver.f90:223-224 */
     int time;
+    /* option 18 (MP_MHD_PML_2D_DISPL, physics2d.f90:719-938), set by orc_set_magnetic */
+    int magnetic;
+    double *box, *boz, *curlboy;           /* nx * nz, B / dimb */
+    double *pmlm, *psipmlm, *scrpmlm;      /* 2 * nx * nzpml: psi of d flux2/dz (induction b_x), of d b_x/dz */
+    double *flux, *bxp, *bzp, *dzbx, *curlby;
 } orc_sim;
 
 static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
@@ -514,7 +519,8 @@ void orc_destroy(orc_sim *s)
                       s->az, s->bzpml, s->axpml, s->bxpml, s->v0x, s->v0z, s->a, s->temp, s->scr,
                       s->pmlvars, s->psipml, s->scrpml, s->pmlvarsx, s->psipmlx, s->scrpmlx,
                       s->dxixdx, s->dxizdz, s->div, s->pp, s->rho, s->gradp_x, s->gradp_z, s->tmp1, s->tmp2,
-                      s->kappa, s->forcing, s->vr, s->fwdsource};
+                      s->kappa, s->forcing, s->vr, s->fwdsource, s->box, s->boz, s->curlboy, s->pmlm,
+                      s->psipmlm, s->scrpmlm, s->flux, s->bxp, s->bzp, s->dzbx, s->curlby};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
     fft_free(&s->fft);
     free(s);
@@ -741,6 +747,155 @@ static void orc_rhs(orc_sim *s)
         }
 }
 
+/* Option 18: the background field (nx * nz, B / dimb, initialize.f90:759) and
+ * curlboy = d box/dz - d boz/dx (physics2d.f90:166-168); switches the step to MP_MHD_PML_2D_DISPL.
+ * The flow must be off (magnetic and flows exclude each other, PARSE_OPTIONS). */
+int orc_set_magnetic(orc_sim *s, const double *box, const double *boz)
+{
+    const size_t N = (size_t)s->nx * s->nz, Np = 2 * (size_t)s->nx * s->nzpml;
+    if (s->p.flows) return -1;
+    if (!s->magnetic) {
+        s->box = zalloc(N); s->boz = zalloc(N); s->curlboy = zalloc(N);
+        s->pmlm = zalloc(Np); s->psipmlm = zalloc(Np); s->scrpmlm = zalloc(Np);
+        s->flux = zalloc(N); s->bxp = zalloc(N); s->bzp = zalloc(N); s->dzbx = zalloc(N); s->curlby = zalloc(N);
+        s->magnetic = 1;
+    }
+    memcpy(s->box, box, N * sizeof(double));
+    memcpy(s->boz, boz, N * sizeof(double));
+    orc_ddz(s, s->box, s->curlboy, 1);
+    orc_ddx_rows(s, s->boz, s->tmp1, s->nz);
+    for (size_t q = 0; q < N; q++) s->curlboy[q] -= s->tmp1[q];
+    return 0;
+}
+
+/* MP_MHD_PML_2D_DISPL (physics2d.f90:719-938): the displacement formulation with the background
+ * field.  As orc_rhs for div xi (ibc 3 with the top preset), the PMLs of psi_vz, psi_vx, p with
+ * d p/dz at ibc 0 (both boundary rows zero, where option 17 uses ibc 2); the field perturbation
+ * b_x = -(d flux2/dz + psi), b_z = d flux2/dx of flux2 = -(xi_x boz - xi_z box); curl b =
+ * d b_x/dz (+ psi) - d b_z/dx; the Lorentz force (curl b boz + curlboy b_z, -curl b box -
+ * curlboy b_x) / rho0; the source as option 17; the bottom row and the first and last columns of
+ * the RHS zero (the top row is not, physics2d.f90:928-935).  The background is laterally
+ * uniform: gradp0_x = gradrho0_x = 0. */
+static void orc18_rhs(orc_sim *s)
+{
+    int nx = s->nx, nz = s->nz, nh = s->p.npmlhor, nhx = s->nhx;
+    size_t N = (size_t)nx * nz, P = (size_t)nx * s->nzpml;
+    const double *T = s->temp;
+    const double *xi_x = T, *xi_z = T + 2 * N, *v_x = T + 3 * N, *v_z = T + 5 * N;
+    double *S = s->scr;
+    double *RHSv_x = S + 3 * N, *RHSv_z = S + 5 * N;
+    double *psivz = s->psipml, *psip = s->psipml + P;
+    double *RHSpsivz = s->scrpml, *RHSpsip = s->scrpml + P;
+    double *psivx = s->psipmlx, *psi_gradp_x = s->psipmlx + (size_t)nhx * nz;
+    double *RHSpsivx = s->scrpmlx, *RHS_psi_gradp_x = s->scrpmlx + (size_t)nhx * nz;
+    double *psiind = s->psipmlm, *psidzbx = s->psipmlm + P;
+    double *RHSpsiind = s->scrpmlm, *RHSpsidzbx = s->scrpmlm + P;
+    double *dxixdx = s->dxixdx, *dxizdz = s->dxizdz;
+
+    orc_ddx_rows(s, xi_x, dxixdx, nz);
+    for (int i = 0; i < nx; i++) dxizdz[(size_t)(nz - 1) * nx + i] = -dxixdx[(size_t)(nz - 1) * nx + i] * s->unstretch[nz - 1];
+    orc_ddz(s, xi_z, dxizdz, 3);
+    for (int k = 0; k < nz; k++) {
+        int pi = pml_index(s, k);
+        if (pi < 0) continue;
+        for (int i = 0; i < nx; i++) {
+            size_t q = (size_t)k * nx + i, qp = (size_t)pi * nx + i;
+            RHSpsivz[qp] = s->az[q] * dxizdz[q] + s->bzpml[q] * psivz[qp];
+            dxizdz[q] = dxizdz[q] + psivz[qp];
+        }
+    }
+    for (int k = 0; k < nz; k++)
+        for (int i = 0; i < nh; i++) {
+            size_t ql = (size_t)k * nx + i, qr = (size_t)k * nx + (nx - nh + i);
+            size_t al = (size_t)k * nhx + i, ar = (size_t)k * nhx + i + nh;
+            dxixdx[ql] = dxixdx[ql] + psivx[al];
+            RHSpsivx[al] = s->axpml[al] * dxixdx[ql] + s->bxpml[al] * psivx[al];
+            dxixdx[qr] = dxixdx[qr] + psivx[ar];
+            RHSpsivx[ar] = s->axpml[ar] * dxixdx[qr] + s->bxpml[ar] * psivx[ar];
+        }
+    for (size_t q = 0; q < N; q++) {
+        s->div[q] = dxixdx[q] + dxizdz[q];
+        s->pp[q] = -s->c2rho0[q] * s->div[q] - s->gradp0_z[q] * xi_z[q];
+        s->rho[q] = -s->rho0[q] * s->div[q] - s->gradrho0_z[q] * xi_z[q];
+    }
+    orc_ddx_rows(s, s->pp, s->gradp_x, nz);
+    memset(s->gradp_z, 0, N * sizeof(double));
+    orc_ddz(s, s->pp, s->gradp_z, 0);
+    for (int k = 0; k < nz; k++) {
+        int pi = pml_index(s, k);
+        if (pi < 0) continue;
+        for (int i = 0; i < nx; i++) {
+            size_t q = (size_t)k * nx + i, qp = (size_t)pi * nx + i;
+            RHSpsip[qp] = s->az[q] * s->gradp_z[q] + s->bzpml[q] * psip[qp];
+            s->gradp_z[q] = s->gradp_z[q] + psip[qp];
+        }
+    }
+    for (int k = 0; k < nz; k++)
+        for (int i = 0; i < nh; i++) {
+            size_t ql = (size_t)k * nx + i, qr = (size_t)k * nx + (nx - nh + i);
+            size_t al = (size_t)k * nhx + i, ar = (size_t)k * nhx + i + nh;
+            s->gradp_x[ql] = s->gradp_x[ql] + psi_gradp_x[al];
+            RHS_psi_gradp_x[al] = s->axpml[al] * s->gradp_x[ql] + s->bxpml[al] * psi_gradp_x[al];
+            s->gradp_x[qr] = s->gradp_x[qr] + psi_gradp_x[ar];
+            RHS_psi_gradp_x[ar] = s->axpml[ar] * s->gradp_x[qr] + s->bxpml[ar] * psi_gradp_x[ar];
+        }
+    for (size_t q = 0; q < N; q++) s->flux[q] = -(xi_x[q] * s->boz[q] - xi_z[q] * s->box[q]);
+    orc_ddz(s, s->flux, s->bxp, 0);
+    orc_ddx_rows(s, s->flux, s->bzp, nz);
+    for (int k = 0; k < nz; k++) {
+        int pi = pml_index(s, k);
+        if (pi < 0) continue;
+        for (int i = 0; i < nx; i++) {
+            size_t q = (size_t)k * nx + i, qp = (size_t)pi * nx + i;
+            RHSpsiind[qp] = s->az[q] * s->bxp[q] + s->bzpml[q] * psiind[qp];
+            s->bxp[q] = s->bxp[q] + psiind[qp];
+        }
+    }
+    for (size_t q = 0; q < N; q++) s->bxp[q] = -s->bxp[q];
+    orc_ddz(s, s->bxp, s->dzbx, 0);
+    orc_ddx_rows(s, s->bzp, s->curlby, nz);
+    for (int k = 0; k < nz; k++) {
+        int pi = pml_index(s, k);
+        if (pi < 0) continue;
+        for (int i = 0; i < nx; i++) {
+            size_t q = (size_t)k * nx + i, qp = (size_t)pi * nx + i;
+            RHSpsidzbx[qp] = s->az[q] * s->dzbx[q] + s->bzpml[q] * psidzbx[qp];
+            s->dzbx[q] = s->dzbx[q] + psidzbx[qp];
+        }
+    }
+    for (int k = 0; k < nz; k++)
+        for (int i = 0; i < nx; i++) {
+            size_t q = (size_t)k * nx + i;
+            const double cb = -s->curlby[q] + s->dzbx[q];
+            RHSv_x[q] = s->rhoinv[q] * (-s->gradp_x[q] + cb * s->boz[q]);
+            RHSv_z[q] = s->rhoinv[q] * (-s->gradp_z[q] - cb * s->box[q]);
+            RHSv_x[q] = RHSv_x[q] + s->rhoinv[q] * (s->curlboy[q] * s->bzp[q]);
+            RHSv_z[q] = RHSv_z[q] + s->rhoinv[q] * (-s->curlboy[q] * s->bxp[q]);
+            RHSv_z[q] = RHSv_z[q] - s->rhoinv[q] * s->rho[q] * s->g[k];
+        }
+    memcpy(S, v_x, N * sizeof(double));
+    memcpy(S + 2 * N, v_z, N * sizeof(double));
+    if (s->time <= s->p.src_until) {
+        if (s->p.adjoint) {
+            int k = s->o_rad;
+            for (int i = 0; i < nx; i++)
+                RHSv_z[(size_t)k * nx + i] += s->forcing[i] * s->delta_width / s->rho0[(size_t)k * nx + i];
+        } else {
+            int k = s->e_rad;
+            double fs = (s->time < s->nfwd) ? s->fwdsource[s->time] : 0.0;
+            for (int i = 0; i < nx; i++)
+                RHSv_z[(size_t)k * nx + i] += s->vr[i] * fs * s->delta_width / s->rho0[(size_t)k * nx + i];
+        }
+    }
+    for (int l = 0; l < 6; l++) {
+        memset(S + (size_t)l * N, 0, nx * sizeof(double));
+        for (int k = 0; k < nz; k++) {
+            S[l * N + (size_t)k * nx + 0] = 0.0;
+            S[l * N + (size_t)k * nx + nx - 1] = 0.0;
+        }
+    }
+}
+
 /* FILTER_VARS_2D, physics2d.f90:509-583 (HORIZONTAL_PMLS: x-FFT filter skipped) */
 static void orc_filter_vars_2d(orc_sim *s)
 {
@@ -787,22 +942,27 @@ void orc_step(orc_sim *s)
 {
     size_t N6 = 6 * (size_t)s->nx * s->nz;
     size_t Np = 2 * (size_t)s->nx * s->nzpml, Nx = 2 * (size_t)s->nhx * s->nz;
+    size_t Nm = s->magnetic ? Np : 0;
     if (s->p.adjoint && s->time <= s->p.src_until) orc_lagrange(s); /* driver.f90:359-360 */
     for (int rk = 0; rk < 5; rk++) {
         if (rk == 0) {
             memcpy(s->temp, s->a, N6 * sizeof(double));
             memcpy(s->psipml, s->pmlvars, Np * sizeof(double));
             memcpy(s->psipmlx, s->pmlvarsx, Nx * sizeof(double));
+            if (Nm) memcpy(s->psipmlm, s->pmlm, Nm * sizeof(double));
         } else {
             double b = s->betas[rk];
             for (size_t q = 0; q < N6; q++) s->temp[q] = s->a[q] + b * s->scr[q];
             for (size_t q = 0; q < Np; q++) s->psipml[q] = s->pmlvars[q] + b * s->scrpml[q];
             for (size_t q = 0; q < Nx; q++) s->psipmlx[q] = s->pmlvarsx[q] + b * s->scrpmlx[q];
+            for (size_t q = 0; q < Nm; q++) s->psipmlm[q] = s->pmlm[q] + b * s->scrpmlm[q];
         }
-        orc_rhs(s);
+        if (s->magnetic) orc18_rhs(s);
+        else orc_rhs(s);
     }
     for (size_t q = 0; q < N6; q++) s->a[q] = s->a[q] + s->deltat * s->scr[q];
     for (size_t q = 0; q < Np; q++) s->pmlvars[q] = s->pmlvars[q] + s->deltat * s->scrpml[q];
+    for (size_t q = 0; q < Nm; q++) s->pmlm[q] = s->pmlm[q] + s->deltat * s->scrpmlm[q];
     orc_filter_vars_2d(s);
     for (size_t q = 0; q < Nx; q++) s->pmlvarsx[q] = s->pmlvarsx[q] + s->deltat * s->scrpmlx[q];
 }
