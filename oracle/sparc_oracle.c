@@ -17,6 +17,8 @@
  * (Fortran i = 1..nx), k = 0..nz-1 (Fortran k = 1..nz, k = 1 the deepest level).
  * The state a(:,:,:,1:6) keeps the six displacement-formulation variables
  * (xi_x, xi_y, xi_z, v_x, v_y, v_z) as in initialize.f90:484-496.
+ * Option 17 (MP_QUIET_PML_2D_DISPL) by default; orc_set_magnetic switches a run without flow to
+ * option 18 (MP_MHD_PML_2D_DISPL, physics2d.f90:719-938), which has no GPU counterpart yet.
  *
  * Build: oracle/Makefile (gcc -O2 -ffp-contract=off, no fast-math) -> oracle/_build/.
  */
