@@ -13,6 +13,7 @@ Modules (reference counterpart in parentheses):
   fdcheck         central-difference check of the exact gradient
   cli, bin/sparc  the `sparc NN MM` executable contract (driver.f90, READ_PARAMETERS)
   full_batched    full.py's per-source loop as one batched process, same files
+  linesearch_batched  linesearch.py's forward runs of all sources and trial models in one batch
   ttadjoint       travel-time adjoint source and misfits (ADJOINT_SOURCE_FILT, MISFIT_ALL)
   gradient, bin/grad.py  gradient post-processing and update directions (grad.py)
   fits, fits_gpu  FITS files and partial-state dumps (all_modules.f90)
