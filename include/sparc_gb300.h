@@ -184,12 +184,14 @@ int sparc_kernels(sparc_plan_t *plan, const void *fsn, int nfwd, const void *asn
 int sparc_kernels_accumulate(sparc_plan_t *plan, const void *fsn, int nfwd, int jf, double *out, void *stream);
 
 /* sparc_kernels_accumulate without any device allocation.  No counterpart in the reference:
- * it serves callers that must not see the library allocate device memory during a run (a
- * caller capturing the adjoint loop in a CUDA graph, or one whose allocator owns all device
- * memory).  Its scratch (the x-derivatives of one record pair, nbatch*4*nz*nx values of the
+ * it serves callers that cannot let the library call cudaMalloc during a run: an embedding host
+ * whose own allocator owns all device memory, or a run whose device-memory budget is fixed
+ * before it starts.  Its scratch (the x-derivatives of one record pair, nbatch*4*nz*nx values of the
  * plan precision) is a file-scope device array of 8 MiB held by every GPU that loads the
  * library until exit; larger batches return SPARC_ERR_SIZE.  The first call on a device looks
- * up the array's address (cudaGetSymbolAddress) and should come before any stream capture.
+ * up the array's address (cudaGetSymbolAddress) and should come before any stream capture; the
+ * address is kept per device index for the life of the process, so a reset of the device's
+ * context (cudaDeviceReset) after that first call is not supported.
  * Every call reuses the same array: calls that overlap on the GPU (other streams, other
  * plans) race and must be serialised by the caller.  Nothing in the array needs clearing: each
  * call writes every element it reads.  Same arguments and results as sparc_kernels_accumulate. */

@@ -2,10 +2,9 @@
 //
 // sparc_kernels_accumulate needs a work buffer for the x-derivatives of one record pair
 // (nbatch x 4 fields x nz x nx of the plan precision) and allocates it with cudaMalloc on
-// first use.  Some callers cannot allow that: a caller that records the adjoint loop into a
-// CUDA graph or runs it under a memory budget fixed before the run, and an embedding host
-// whose allocator owns every device allocation, must not see the library allocate in the
-// middle of a run.  sparc_kernels_accumulate_static serves them: its scratch is the
+// first use.  Some callers cannot allow that: an embedding host whose allocator owns every
+// device allocation, or a run whose device-memory budget is fixed before it starts, must not
+// see the library call cudaMalloc in the middle of a run.  sparc_kernels_accumulate_static serves them: its scratch is the
 // file-scope device array below, fixed in size and held by every GPU that loads the library
 // until the process exits.
 #include <cstdio>
@@ -27,7 +26,8 @@ constexpr int MAX_DEVICES = 64;
 std::mutex g_mu;
 void *g_scratch_addr[MAX_DEVICES] = {};
 
-// Device address of g_static_scratch on the current device (looked up once per device).
+// Device address of g_static_scratch on the current device (looked up once per device index
+// and kept for the life of the process: a context reset after the first call is unsupported).
 cudaError_t scratch_address(void **out)
 {
     int dev = 0;

@@ -1,5 +1,6 @@
 """sparc_kernels_accumulate_static: the kernel-integral accumulation for callers that must not
-see the library allocate device memory mid-run (graph-capturing or fixed-budget callers).  It
+see the library call cudaMalloc mid-run (an embedding host whose allocator owns all device
+memory, or a run with a device-memory budget fixed before it starts).  It
 must give the same sums as sparc_kernels_accumulate, whose work buffer is allocated on first
 use, call after call.  Runs alone in a fresh process or after the rest of the suite."""
 import ctypes
