@@ -179,6 +179,22 @@ def cpu_baseline_quick():
             "sample": f"{nsolve} FP64 forward solves x {steps} steps of the batch32 grid on {nsolve} host threads"}
 
 
+def plain64_oracle_records(nsteps):
+    """Seismograms of the plain FP64 workload from the FP64 oracle (the checker of the fp64_plain
+    figure); runs in a spawned process while the GPU is timed."""
+    from oracle import oracle as O
+    from sparc_flows_gb300 import model as M
+
+    run, model, specs, _, _ = M.workload("plain64")
+    run = run.replace(nsteps=nsteps)
+    sp = specs[0]
+    sim = O.OracleSim(run, model)
+    sim.set_forward_source(sp.xloc, sp.spatial, sp.sigma, sp.temporal, sp.nu0, run.nsteps + 8)
+    seis = sim.run_steps(run.nsteps)
+    sim.close()
+    return seis
+
+
 def gradient_stage(pipe, model, dev, reps=20, cpu=True):
     """The gradient post-processing of grad.py on this batch's own kernels: sparc_gradient (kernel
     sum, hessian preconditioning, x/z filters, antisymmetrisation), a conjugate-gradient direction
@@ -296,6 +312,14 @@ def run_gpu(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    # the oracle's plain64 records (the fp64_plain figure's checker), computed on one host core in
+    # a spawned process while the GPU runs; started before the first CUDA call
+    oracle_job = None
+    if rank == 0 and not args.no_plain and not args.no_cpu:
+        import concurrent.futures as cf
+        import multiprocessing as mp
+        pool = cf.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn"))
+        oracle_job = (pool, pool.submit(plain64_oracle_records, min(args.nsteps or 1800, 1800)))
     if world > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
@@ -353,8 +377,16 @@ def run_gpu(args):
         torch.cuda.synchronize()
         pms = q0.elapsed_time(q1) / 2
         plain = {"workload": "plain64: 1 source, nx=256 (200 Mm), nz=300, no flow, 1800 steps, FP64",
-                 "value": pp.point_steps() / (pms * 1e-3), "unit": UNIT, "ms_per_run": pms}
+                 "value": pp.point_steps() / (pms * 1e-3), "unit": UNIT, "ms_per_run": pms,
+                 "column_kernel": pp.fwd.column_kernel_name()}
+        plain_seis = pp.seis[0].double().cpu().numpy()
         pp.close()
+        if oracle_job is not None:
+            pool, fut = oracle_job
+            ref = fut.result()
+            pool.shutdown()
+            plain["seismograms_rel_l2_vs_oracle"] = float(np.linalg.norm(plain_seis - ref) / np.linalg.norm(ref))
+            plain["oracle"] = "FP64 CPU restatement (physics2d.f90:943-1094, step.f90:43-119), same inputs"
 
     # ---- end-to-end through the public API: pinned host inputs in, host kernels/seismograms out
     nrec = run.nrec

@@ -55,9 +55,10 @@ typedef struct {
     int compensated;           /* FP32 plans: 1 keeps a low-order part of the state so the RK
                                   update and filter round like FP64 arithmetic (no reference
                                   counterpart; the reference state is FP64) */
-    int column_block;          /* column-pass block width in x-columns (tuning): 32 or 8 for the
-                                  partitioned solve (other values: 32), 32, 16 or 8 for the banded
-                                  pass (other values: 16) */
+    int column_block;          /* column-pass block width in x-columns (tuning): 32, 8 or 4 for
+                                  the partitioned solve (other values: the widest whose blocks
+                                  fill the GPU, down to 4), 32, 16 or 8 for the banded pass
+                                  (other values: 32) */
     int column_impl;           /* column pass: 0 partitioned solve with direct loads, 1 partitioned
                                   solve with TMA-staged tiles, 2 (FP32 plans) geometric-band
                                   inverse of the compact operator with direct loads, 3 (FP32 plans)

@@ -598,7 +598,16 @@ int alloc_solver(sparc_plan *p)
     a.d_time = p->d_time;
     a.src_until = c.src_until; a.k_inj = c.k_inj; a.k_obs = c.k_obs; a.steps_out = c.steps_out;
     a.filt_k0 = c.filter_k0; a.filt_xall = c.filter_all_x;
-    a.colw = (c.column_block != 8 && nx % 32 == 0) ? 32 : 8;
+    // partitioned-solve block width: 32, 8 or 4 columns on request; otherwise the widest whose
+    // blocks (nx / width per solve) fill the 152 SMs, down to 4 (one FP64 sector per row), so a
+    // single 256-column solve still spreads over 64 SMs
+    if ((c.column_block == 32 || c.column_block == 8 || c.column_block == 4) && nx % c.column_block == 0) {
+        a.colw = c.column_block;
+    } else {
+        a.colw = 4;
+        for (int w : {32, 8})
+            if (nx % w == 0 && (long long)(nx / w) * nb >= 152) { a.colw = w; break; }
+    }
     a.inj_scale = inj; a.src_rows = rows; a.nrows = 1;
     a.d_err = p->d_err;
     {  // streamed end-of-step kernel: two [nz][32] fields in shared memory
@@ -609,7 +618,7 @@ int alloc_solver(sparc_plan *p)
     }
     // banded column pass (FP32 only: its truncation at 5e-10 is below FP32 rounding, not FP64's)
     S.band_R = 0;
-    const int bcw = (c.column_block == 8 || c.column_block == 16 || c.column_block == 32) ? c.column_block : 16;
+    const int bcw = (c.column_block == 8 || c.column_block == 16 || c.column_block == 32) ? c.column_block : 32;
     if (sizeof(T) == 4 && (c.column_impl == 2 || c.column_impl == 3) && nx % bcw == 0 && col_band_rows(nz, bcw) > 0) {
         const int R = col_band_rows(nz, bcw);
         int maxsm = 0, dev = 0;

@@ -553,10 +553,11 @@ static cudaError_t launch_kacc_cw(const KAccArgs<T> &a, cudaStream_t st)
 template <typename T>
 cudaError_t launch_kacc(const KAccArgs<T> &a, cudaStream_t st)
 {
-    if (a.nx % a.colw || a.L > ColCfg<T>::LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
+    const int cw = a.colw == 32 ? 32 : 8;
+    if (a.nx % cw || a.L > ColCfg<T>::LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
     cudaError_t e = launch_kacc_row<T>(a, st);
     if (e != cudaSuccess) return e;
-    return a.colw == 32 ? launch_kacc_cw<T, 32>(a, st) : launch_kacc_cw<T, 8>(a, st);
+    return cw == 32 ? launch_kacc_cw<T, 32>(a, st) : launch_kacc_cw<T, 8>(a, st);
 }
 template cudaError_t launch_kacc<float>(const KAccArgs<float> &, cudaStream_t);
 template cudaError_t launch_kacc<double>(const KAccArgs<double> &, cudaStream_t);
@@ -577,7 +578,12 @@ template <typename T>
 cudaError_t launch_col_stage(const StepArgs<T> &a, cudaStream_t st)
 {
     if (a.nx % a.colw || a.L > ColCfg<T>::LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
-    return a.colw == 32 ? launch_col_stage_cw<T, 32>(a, st) : launch_col_stage_cw<T, 8>(a, st);
+    switch (a.colw) {
+        case 32: return launch_col_stage_cw<T, 32>(a, st);
+        case 8: return launch_col_stage_cw<T, 8>(a, st);
+        case 4: return launch_col_stage_cw<T, 4>(a, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 template <typename T, int CW>
@@ -595,8 +601,9 @@ static cudaError_t launch_end_step_cw(const StepArgs<T> &a, cudaStream_t st)
 template <typename T>
 cudaError_t launch_end_step(const StepArgs<T> &a, cudaStream_t st)
 {
-    if (a.nx % a.colw || a.L > ColCfg<T>::LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
-    return a.colw == 32 ? launch_end_step_cw<T, 32>(a, st) : launch_end_step_cw<T, 8>(a, st);
+    const int cw = a.colw == 32 ? 32 : 8;
+    if (a.nx % cw || a.L > ColCfg<T>::LMAX || a.nch > ColCfg<T>::MAXNCH) return cudaErrorInvalidValue;
+    return cw == 32 ? launch_end_step_cw<T, 32>(a, st) : launch_end_step_cw<T, 8>(a, st);
 }
 
 template <typename T, int CW>

@@ -128,7 +128,7 @@ class WaveSolver:
         cfg.compensated = int(os.environ.get("SPARC_COMPENSATED", "0"))
         impl, block = self._column
         cfg.column_impl = int(os.environ.get("SPARC_COLUMN_IMPL", "2")) if impl is None else int(impl)
-        cfg.column_block = int(os.environ.get("SPARC_COLUMN_BLOCK", "32")) if block is None else int(block)
+        cfg.column_block = int(os.environ.get("SPARC_COLUMN_BLOCK", "0")) if block is None else int(block)
         self.cfg = cfg
         h = ctypes.c_void_p()
         capi.check(self.L.sparc_plan_create(ctypes.byref(cfg), ctypes.byref(h)), "sparc_plan_create")
