@@ -56,13 +56,15 @@ typedef struct {
                                   update and filter round like FP64 arithmetic (no reference
                                   counterpart; the reference state is FP64) */
     int column_block;          /* column-pass block width in x-columns (tuning): 32, 8 or 4 for
-                                  the partitioned solve (other values: the widest whose blocks
-                                  fill the GPU, down to 4), 32, 16 or 8 for the banded pass
+                                  the partitioned solve (other values: 32 if nbatch * nx / 32
+                                  blocks fill the GPU, else 8), 32, 16 or 8 for the banded pass
                                   (other values: 32) */
     int column_impl;           /* column pass: 0 partitioned solve with direct loads, 1 partitioned
                                   solve with TMA-staged tiles, 2 (FP32 plans) geometric-band
-                                  inverse of the compact operator with direct loads, 3 (FP32 plans)
-                                  geometric band with TMA-staged tiles; FP64 plans use 0 for 2, 3 */
+                                  inverse of the compact operator with direct loads (five phases,
+                                  two derivatives each), 3 (FP32 plans) geometric band with
+                                  TMA-staged tiles, 4 (FP32 plans) geometric band in seven phases;
+                                  FP64 plans use 0 for 2, 3, 4 */
 } sparc_config_t;
 
 /* Background, all DEVICE pointers to FP64 arrays; copied (and rounded for FP32 plans) into

@@ -49,6 +49,17 @@ __device__ __forceinline__ void band_rhs(const ZTab<float> &tb, const float *Fc,
                                          int nz, float preset, float (&rhs)[R])
 {
     float w[R + 4];  // rows k0-2 .. k0+R+1
+    if (k0 >= 2 && k0 + R + 2 <= nz) {  // every row of the group interior (uniform over the group)
+#pragma unroll
+        for (int i = 0; i < R + 4; i++) w[i] = Fc[(k0 - 2 + i) * CW + c];
+#pragma unroll
+        for (int m = 0; m < R; m++) {
+            const float v = tb.c1 * (w[m + 3] - w[m + 1]) + tb.c2 * (w[m + 4] - w[m]);
+            Rc[(k0 + m) * CW + c] = v;
+            rhs[m] = v;
+        }
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < R + 4; i++) {
         const int k = k0 - 2 + i;

@@ -598,15 +598,14 @@ int alloc_solver(sparc_plan *p)
     a.d_time = p->d_time;
     a.src_until = c.src_until; a.k_inj = c.k_inj; a.k_obs = c.k_obs; a.steps_out = c.steps_out;
     a.filt_k0 = c.filter_k0; a.filt_xall = c.filter_all_x;
-    // partitioned-solve block width: 32, 8 or 4 columns on request; otherwise the widest whose
-    // blocks (nx / width per solve) fill the 152 SMs, down to 4 (one FP64 sector per row), so a
-    // single 256-column solve still spreads over 64 SMs
+    // partitioned-solve block width: 32, 8 or 4 columns on request; otherwise 32 when those blocks
+    // (nx / 32 per solve) fill the 152 SMs, else 8.  One FP64 solve of 256 columns (the plain
+    // configuration): column pass 0.66 ms per step at 32 columns (8 blocks), 0.33 at 8 (32
+    // blocks), 0.35 at 4 (64 blocks, 76 threads each) on a GB300
     if ((c.column_block == 32 || c.column_block == 8 || c.column_block == 4) && nx % c.column_block == 0) {
         a.colw = c.column_block;
     } else {
-        a.colw = 4;
-        for (int w : {32, 8})
-            if (nx % w == 0 && (long long)(nx / w) * nb >= 152) { a.colw = w; break; }
+        a.colw = (nx % 32 == 0 && (long long)(nx / 32) * nb >= 152) ? 32 : 8;
     }
     a.inj_scale = inj; a.src_rows = rows; a.nrows = 1;
     a.d_err = p->d_err;
@@ -619,7 +618,9 @@ int alloc_solver(sparc_plan *p)
     // banded column pass (FP32 only: its truncation at 5e-10 is below FP32 rounding, not FP64's)
     S.band_R = 0;
     const int bcw = (c.column_block == 8 || c.column_block == 16 || c.column_block == 32) ? c.column_block : 32;
-    if (sizeof(T) == 4 && (c.column_impl == 2 || c.column_impl == 3) && nx % bcw == 0 && col_band_rows(nz, bcw) > 0) {
+    a.band_phases = c.column_impl == 4 ? 7 : 5;
+    if (sizeof(T) == 4 && (c.column_impl == 2 || c.column_impl == 3 || c.column_impl == 4) && nx % bcw == 0 &&
+        col_band_rows(nz, bcw) > 0) {
         const int R = col_band_rows(nz, bcw);
         int maxsm = 0, dev = 0;
         cudaGetDevice(&dev);
@@ -1228,7 +1229,8 @@ int sparc_plan_describe(const sparc_plan_t *p, char *buf, int len)
         const Solver<float> &S = p->s32;
         if (S.band_tma_R) col = "col_band_tma_kernel<" + std::to_string(S.band_tma_R) + ">";
         else if (S.band_R)
-            col = "col_band_kernel<" + std::to_string(S.band_cw) + "," + std::to_string(S.band_R) + "," +
+            col = std::string(S.a.band_phases == 7 ? "col_band_kernel<" : "col_band5_kernel<") +
+                  std::to_string(S.band_cw) + "," + std::to_string(S.band_R) + "," +
                   (col_band_specialised(p->cfg.nx, p->cfg.nz, S.band_cw, S.band_R)
                        ? std::to_string(p->cfg.nx) + "," + std::to_string(p->cfg.nz)
                        : std::string("0,0")) +

@@ -63,6 +63,7 @@ struct StepArgs {
     int src_until, k_inj, k_obs, steps_out;
     int filt_k0, filt_xall;  // FILTER_VARS_2D coverage (rows from filt_k0, all columns if filt_xall)
     int colw;                // column-pass block width (8 or 32 columns)
+    int band_phases;         // banded column pass: 5 (two derivatives per phase) or 7 phases
     int boxr;                // rows per TMA box of the staged column pass (2 boxes cover nz)
     int *d_err;              // device error flag (SPARC_DEV_ERR_*)
     const T *inj_scale, *src_rows;
