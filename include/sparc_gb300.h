@@ -186,6 +186,19 @@ int sparc_kernels(sparc_plan_t *plan, const void *fsn, int nfwd, const void *asn
  * dumps and their re-reading (all_modules.f90:750-784, kernels.f90:258-280). */
 int sparc_kernels_accumulate(sparc_plan_t *plan, const void *fsn, int nfwd, int jf, double *out, void *stream);
 
+/* The adjoint stage of one iteration: the reference's sparc run with the Adjoint instruction
+ * (TIMESTEPPING with the flow negated and the Lagrange-interpolated adjoint source, driver.f90:
+ * 144-147, 337-475, 584-594; physics.f90:678-737) followed by its kernel stage (PRODUCE_KERNELS,
+ * kernels.f90:209-358), without the partial-state dumps between the two.  The plan must be set up
+ * for the adjoint (k_inj = o_rad) with its adjoint source already uploaded by sparc_set_source
+ * (the residual as source rows, the LAGRANGE_INTERP weights as the table).  Resets the plan,
+ * zeroes out (DEVICE FP64 [nbatch][4][nz][nx]), then advances nsteps steps; after the step that
+ * writes adjoint record ja (ja = 0 .. nfwd-1, at time ja*steps_out, the first after one step) the
+ * integrands of adjoint v_x, v_z against forward record nfwd-1-ja of fsn ([nbatch][nfwd][6][nz][nx],
+ * DEVICE, plan precision, as written by sparc_forward) are accumulated into out as
+ * sparc_kernels_accumulate does.  Needs 1 + (nfwd-1)*steps_out <= nsteps.  Stream-ordered. */
+int sparc_adjoint(sparc_plan_t *plan, const void *fsn, int nfwd, int nsteps, double *out, void *stream);
+
 /* sparc_kernels_accumulate without any device allocation.  No counterpart in the reference:
  * it serves callers that cannot let the library call cudaMalloc during a run: an embedding host
  * whose own allocator owns all device memory, or a run whose device-memory budget is fixed

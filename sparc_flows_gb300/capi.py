@@ -47,6 +47,7 @@ SIGNATURES = {
     "sparc_kernels": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_kernels_accumulate": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_kernels_accumulate_static": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
+    "sparc_adjoint": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp]),
     "sparc_zband_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _dp]),
     "sparc_zsolve_host": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, ctypes.c_int]),
     "sparc3d_plan_create": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),

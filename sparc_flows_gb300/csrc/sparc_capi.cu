@@ -1355,6 +1355,41 @@ int sparc_kernels_accumulate(sparc_plan_t *p, const void *fsn, int nfwd, int jf,
     return kernels_impl<double>(p, fsn, nfwd, p->s64.a.A + 2 * F, (long long)4 * F, jf, out, (cudaStream_t)stream);
 }
 
+int sparc_adjoint(sparc_plan_t *p, const void *fsn, int nfwd, int nsteps, double *out, void *stream)
+{
+    if (!p || !fsn || !out || nfwd < 1 || nsteps < 1) return fail(SPARC_ERR_ARG, "sparc_adjoint: bad argument");
+    if (!p->have_bg || !p->have_src) return fail(SPARC_ERR_STATE, "sparc_adjoint: background and source must be set first");
+    const int so = p->cfg.steps_out;
+    if (so < 1 || 1 + (long long)(nfwd - 1) * so > nsteps)
+        return fail(SPARC_ERR_ARG, "sparc_adjoint: nfwd records need 1 + (nfwd - 1) * steps_out <= nsteps");
+    const cudaStream_t st = (cudaStream_t)stream;
+    const bool f32 = p->cfg.precision == 32;
+    const size_t F = (size_t)p->cfg.nx * p->cfg.nz;
+    int rc = f32 ? reset_state<float>(p, 0, st) : reset_state<double>(p, 0, st);
+    if (rc != SPARC_OK) return rc;
+    CK(cudaMemsetAsync(out, 0, (size_t)p->cfg.nbatch * 4 * F * sizeof(double), st));
+    // adjoint record ja (written at time ja * steps_out, the first after one step) pairs with
+    // forward record nfwd - 1 - ja (kernels.f90:215, 258)
+    int done = 0;
+    for (int ja = 0; ja < nfwd; ja++) {
+        const int n = ja == 0 ? 1 : so;
+        rc = f32 ? run_forward<float>(p, n, -1.0, nullptr, nullptr, 0, 0, 1, st)
+                 : run_forward<double>(p, n, -1.0, nullptr, nullptr, 0, 0, 1, st);
+        if (rc != SPARC_OK) return rc;
+        done += n;
+        const int jf = nfwd - 1 - ja;
+        rc = f32 ? kernels_impl<float>(p, fsn, nfwd, p->s32.a.A + 2 * F, (long long)4 * F, jf, out, st)
+                 : kernels_impl<double>(p, fsn, nfwd, p->s64.a.A + 2 * F, (long long)4 * F, jf, out, st);
+        if (rc != SPARC_OK) return rc;
+    }
+    if (nsteps > done) {
+        rc = f32 ? run_forward<float>(p, nsteps - done, -1.0, nullptr, nullptr, 0, 0, 1, st)
+                 : run_forward<double>(p, nsteps - done, -1.0, nullptr, nullptr, 0, 0, 1, st);
+        if (rc != SPARC_OK) return rc;
+    }
+    return SPARC_OK;
+}
+
 int sparc_kernels_accumulate_static(sparc_plan_t *p, const void *fsn, int nfwd, int jf, double *out, void *stream)
 {
     if (!p || !fsn || !out || nfwd < 1 || jf < 0 || jf >= nfwd)

@@ -110,6 +110,9 @@ class FwdAdjKernels:
         """Adjoint solve with kernel accumulation at each record (kernels.f90:209-358)."""
         run, so = self.run, self.run.steps_out
         self.adj.set_adjoint_sources_device(src)
+        if not self.ck:  # every forward record is resident: the library runs the whole loop
+            self.adj.adjoint_with_kernels(self.snaps, self.kacc, run.nsteps)
+            return
         self.adj.reset(0)
         self.kacc.zero_()
         done = 0

@@ -333,6 +333,15 @@ class WaveSolver:
         capi.check(self.L.sparc_kernels_accumulate(self.plan, _ptr(fsnaps), fsnaps.shape[1], jf, _ptr(out),
                                                    _stream()), "sparc_kernels_accumulate")
 
+    def adjoint_with_kernels(self, fsnaps: torch.Tensor, out: torch.Tensor, nsteps: int | None = None):
+        """The whole adjoint run with the kernel integral (sparc_adjoint): from rest, nsteps steps
+        with the flow negated; after each adjoint record, its v_x, v_z against the matching forward
+        record of fsnaps (nb, nfwd, 6, nz, nx) accumulated into out (nb, 4, nz, nx) FP64 (zeroed
+        first).  The adjoint source must be set."""
+        nsteps = self.run.nsteps if nsteps is None else nsteps
+        capi.check(self.L.sparc_adjoint(self.plan, _ptr(fsnaps), fsnaps.shape[1], nsteps, _ptr(out), _stream()),
+                   "sparc_adjoint")
+
     def reset(self, time0: int = 0):
         capi.check(self.L.sparc_reset_state(self.plan, time0, _stream()), "sparc_reset_state")
 
