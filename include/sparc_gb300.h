@@ -61,10 +61,8 @@ typedef struct {
                                   (other values: 32) */
     int column_impl;           /* column pass: 0 partitioned solve with direct loads, 1 partitioned
                                   solve with TMA-staged tiles, 2 (FP32 plans) geometric-band
-                                  inverse of the compact operator with direct loads (five phases,
-                                  two derivatives each), 3 (FP32 plans) geometric band with
-                                  TMA-staged tiles, 4 (FP32 plans) geometric band in seven phases;
-                                  FP64 plans use 0 for 2, 3, 4 */
+                                  inverse of the compact operator with direct loads, 3 (FP32 plans)
+                                  geometric band with TMA-staged tiles; FP64 plans use 0 for 2, 3 */
 } sparc_config_t;
 
 /* Background, all DEVICE pointers to FP64 arrays; copied (and rounded for FP32 plans) into

@@ -618,14 +618,12 @@ int alloc_solver(sparc_plan *p)
     // banded column pass (FP32 only: its truncation at 5e-10 is below FP32 rounding, not FP64's)
     S.band_R = 0;
     const int bcw = (c.column_block == 8 || c.column_block == 16 || c.column_block == 32) ? c.column_block : 32;
-    a.band_phases = c.column_impl == 4 ? 7 : 5;
-    if (sizeof(T) == 4 && (c.column_impl == 2 || c.column_impl == 3 || c.column_impl == 4) && nx % bcw == 0 &&
-        col_band_rows(nz, bcw) > 0) {
+    if (sizeof(T) == 4 && (c.column_impl == 2 || c.column_impl == 3) && nx % bcw == 0 && col_band_rows(nz, bcw) > 0) {
         const int R = col_band_rows(nz, bcw);
         int maxsm = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        bool ok = col_band_smem_bytes(nz, R, bcw) <= (size_t)maxsm;
+        bool ok = col_band_smem_bytes(nz, nzpml, R, bcw) <= (size_t)maxsm;
         HostBand hb[3];
         for (int i = 0; i < 3 && ok; i++) ok = build_band(p->hz[i + 1], hb[i]);
         for (int i = 1; i < 3 && ok; i++)  // the interior operator does not depend on the boundary condition
@@ -1229,8 +1227,7 @@ int sparc_plan_describe(const sparc_plan_t *p, char *buf, int len)
         const Solver<float> &S = p->s32;
         if (S.band_tma_R) col = "col_band_tma_kernel<" + std::to_string(S.band_tma_R) + ">";
         else if (S.band_R)
-            col = std::string(S.a.band_phases == 7 ? "col_band_kernel<" : "col_band5_kernel<") +
-                  std::to_string(S.band_cw) + "," + std::to_string(S.band_R) + "," +
+            col = "col_band_kernel<" + std::to_string(S.band_cw) + "," + std::to_string(S.band_R) + "," +
                   (col_band_specialised(p->cfg.nx, p->cfg.nz, S.band_cw, S.band_R)
                        ? std::to_string(p->cfg.nx) + "," + std::to_string(p->cfg.nz)
                        : std::string("0,0")) +

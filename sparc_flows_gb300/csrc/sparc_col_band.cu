@@ -29,6 +29,10 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     float *KPB = RB + (size_t)nz * CW + 2 * ncar;
     float *Kst = KPB, *Kri = KPB + nz, *Kr0 = KPB + 2 * nz, *Kgp = KPB + 3 * nz, *Kgr = KPB + 4 * nz, *Kg = KPB + 5 * nz,
           *Kc2 = KPB + 6 * nz;
+    // vertical-PML inputs of this block's PML rows [5][nzpml][CW]: stage inputs of psi_vz and psi_p
+    // (replaced by their new RHS once used), az, bz, fdz
+    const int nzp = a.nzpml;
+    float *PS = KPB + 7 * nz;
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {  // depth profiles
         Kst[k] = __ldg(a.stretch + k);
         Kri[k] = __ldg(a.rhoinv + k);
@@ -48,6 +52,36 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     const int s = a.stage;
     const float bs = a.bs, bsm1 = a.bsm1;
     const int time = *a.d_time;
+    const bool xbc = (x == 0 || x == nx - 1);
+    // does this thread group hold vertical-PML rows (uniform over the group: a warp for CW = 32)
+    const bool pml_group = k0 < a.npmlbot || k0 + n > nz - a.npmltop;
+    const size_t spz_slot = (size_t)a.nb * 2 * nzp * nx;  // one slot of the PML RHS ring
+
+    // Global stores wait until the loads of their phase are issued (every phase below loads,
+    // computes into registers or shared memory, and stores last), so that the loads of one row
+    // never queue behind a possibly aliasing store of the previous row.
+
+    // ---- 0: PML inputs of the thread's own rows into shared memory (only the thread reads them)
+    if (pml_group) {
+#pragma unroll
+        for (int m = 0; m < R; m++) {
+            const int pi = m < n ? pml_row(a, k0 + m) : -1;
+            if (pi >= 0) {
+                const size_t qz = ((size_t)b * 2 * nzp + pi) * nx + x;  // psi_vz; psi_p at + nzp * nx
+                const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
+                float p0 = __ldg(a.PZ + qz), p1 = __ldg(a.PZ + qz + (size_t)nzp * nx);
+                if (s >= 2) {
+                    p0 += bs * __ldg(a.SPZ + a.slot_sm1 * spz_slot + qz);
+                    p1 += bs * __ldg(a.SPZ + a.slot_sm1 * spz_slot + qz + (size_t)nzp * nx);
+                }
+                PS[(0 * nzp + pi) * CW + c] = p0;
+                PS[(1 * nzp + pi) * CW + c] = p1;
+                PS[(2 * nzp + pi) * CW + c] = __ldg(a.az + qb);
+                PS[(3 * nzp + pi) * CW + c] = __ldg(a.bz + qb);
+                PS[(4 * nzp + pi) * CW + c] = __ldg(a.fdz + qb);
+            }
+        }
+    }
 
     // L2 prefetch of the later phases' per-point inputs of this thread group's rows: one
     // 128-byte line per (array, row) for CW = 32, spread over the lanes, no registers held, so
@@ -84,7 +118,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
             if (s >= 2) {
                 const float avz = __ldg(Ab + F_VZ * F + q);
                 float t = (s == 2) ? avz : avz + bsm1 * __ldg(svp(a, a.slot_sm2, b, 1) + q);
-                if (k == 0 || x == 0 || x == nx - 1) t = 0.f;
+                if (k == 0 || xbc) t = 0.f;
                 v += bs * t;
             }
             xz[m] = v;
@@ -100,7 +134,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         band_publish<CW, R>(bd, bd.uv[2], C0, c, g, k0, n, nz, ra);
     }
     __syncthreads();
-    // ---- 3: d xi_z/dz, vertical PML, divergence, pressure; v_x of stage s
+    // ---- 3: d xi_z/dz, vertical PML, divergence, pressure (kept in FA); v_x of stage s
     {
         float d[R];
         band_eval<CW, R>(bd, bd.uv[2], C0, c, g, G, k0, n, nz, RA, d);
@@ -110,17 +144,13 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
                 const int k = k0 + m;
                 const size_t q = (size_t)k * nx + x;
                 float dzz = d[m] * Kst[k];
-                const int pi = pml_row(a, k);
+                const int pi = pml_group ? pml_row(a, k) : -1;
                 float fd = 1.f;
                 if (pi >= 0) {
-                    const size_t qz = ((size_t)b * 2 * a.nzpml + pi) * nx + x;  // psi_vz
-                    const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
-                    float ps = __ldg(a.PZ + qz);
-                    if (s >= 2) ps += bs * __ldg(a.SPZ + (size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz);
-                    a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz] =
-                        __ldg(a.az + qb) * dzz + __ldg(a.bz + qb) * ps;
+                    const float ps = PS[(0 * nzp + pi) * CW + c];
+                    PS[(0 * nzp + pi) * CW + c] = PS[(2 * nzp + pi) * CW + c] * dzz + PS[(3 * nzp + pi) * CW + c] * ps;
                     dzz += ps;
-                    fd = __ldg(a.fdz + qb);
+                    fd = PS[(4 * nzp + pi) * CW + c];
                 }
                 const float div = __ldg(a.DX + (size_t)b * F + q) + dzz;
                 const float c2r = a.c2d ? __ldg(a.c2rho0 + (size_t)b * a.bg2 + q) : Kc2[k];
@@ -129,7 +159,6 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
                 const float rho = -Kr0[k] * div - gr * xz[m];
                 xz[m] = rho * Kg[k];
                 FA[k * CW + c] = p;
-                a.P[(size_t)b * F + q] = p;
                 float vx = __ldg(Ab + F_VX * F + q);
                 if (s >= 2) vx += bs * __ldg(svp(a, a.slot_sm1, b, 0) + q);
                 FB[k * CW + c] = vx;
@@ -137,7 +166,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         }
     }
     __syncthreads();
-    // ---- 4: right-hand sides of dp/dz (ibc 2, bottom value 0) and dv_x/dz (ibc 1)
+    // ---- 4: right-hand sides of dp/dz (ibc 2, bottom value 0) and dv_x/dz (ibc 1); p to HBM
     {
         float rr[R];
         band_rhs<CW, R>(a.z2, FA, RA, c, k0, n, nz, 0.f, rr);
@@ -148,8 +177,12 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         band_rhs<CW, R>(a.z1, FB, RB, c, k0, n, nz, 0.f, rr);
         band_publish<CW, R>(bd, bd.uv[0], C1, c, g, k0, n, nz, rr);
     }
+#pragma unroll
+    for (int m = 0; m < R; m++)
+        if (m < n) a.P[(size_t)b * F + (size_t)(k0 + m) * nx + x] = FA[(k0 + m) * CW + c];
     __syncthreads();
-    // ---- 5: gradient of p, RHS v_z without advection; advection of v_x along z; v_z of stage s
+    // ---- 5: gradient of p, RHS v_z without advection; advection of v_x along z (partial RHS
+    // v_x kept in FB); v_z of stage s
     {
         float d[R];
         band_eval<CW, R>(bd, bd.uv[1], C0, c, g, G, k0, n, nz, RA, d, true);
@@ -158,14 +191,10 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
             if (m < n) {
                 const int k = k0 + m;
                 float gpz = d[m] * Kst[k];
-                const int pi = pml_row(a, k);
+                const int pi = pml_group ? pml_row(a, k) : -1;
                 if (pi >= 0) {
-                    const size_t qz = (((size_t)b * 2 + 1) * a.nzpml + pi) * nx + x;  // psi_p
-                    const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
-                    float ps = __ldg(a.PZ + qz);
-                    if (s >= 2) ps += bs * __ldg(a.SPZ + (size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz);
-                    a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz] =
-                        __ldg(a.az + qb) * gpz + __ldg(a.bz + qb) * ps;
+                    const float ps = PS[(1 * nzp + pi) * CW + c];
+                    PS[(1 * nzp + pi) * CW + c] = PS[(2 * nzp + pi) * CW + c] * gpz + PS[(3 * nzp + pi) * CW + c] * ps;
                     gpz += ps;
                 }
                 xz[m] = -Kri[k] * (gpz + xz[m]);
@@ -182,11 +211,11 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
                     const float dvxdz = d[m] * Kst[k];
                     rv = __ldg(a.FXX + (size_t)b * F + q) -
                          2.f * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvxdz;
+                    float vz = __ldg(Ab + F_VZ * F + q);
+                    if (s >= 2) vz += bs * __ldg(svp(a, a.slot_sm1, b, 1) + q);
+                    FA[k * CW + c] = vz;
                 }
-                a.RVXP[(size_t)b * F + q] = rv;
-                float vz = __ldg(Ab + F_VZ * F + q);
-                if (s >= 2) vz += bs * __ldg(svp(a, a.slot_sm1, b, 1) + q);
-                FA[k * CW + c] = vz;
+                FB[k * CW + c] = rv;
             }
         }
     }
@@ -198,7 +227,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         band_publish<CW, R>(bd, bd.uv[0], C0, c, g, k0, n, nz, rr);
         __syncthreads();
     }
-    // ---- 7: finish RHS v_z (advection, source, boundary zeros)
+    // ---- 7: finish RHS v_z (advection, source, boundary zeros); this stage's stores
     float d[R];
     if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C0, c, g, G, k0, n, nz, RA, d, true);
     float forcing = 0.f;
@@ -214,7 +243,6 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         }
         forcing = (float)f * __ldg(a.inj_scale + (size_t)b * nx + x);
     }
-    float *svz = svp(a, a.slot_s, b, 1);
 #pragma unroll
     for (int m = 0; m < R; m++) {
         if (m < n) {
@@ -226,227 +254,28 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
                 const float dvzdz = d[m] * Kst[k];
                 r += __ldg(a.FXZ + (size_t)b * F + q) - 2.f * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvzdz;
             }
-            if (k == 0 || x == 0 || x == nx - 1) r = 0.f;
-            svz[q] = r;
+            if (k == 0 || xbc) r = 0.f;
+            xz[m] = r;
         }
     }
-}
-
-// The same stage in five phases and four barriers: the derivatives that do not depend on the
-// pressure (d xi_z/dz, d v_x/dz) share phases 2-3, and d p/dz and d v_z/dz share phases 4-5, so
-// every evaluation phase runs two independent band evaluations.  Shared memory as
-// col_band_kernel: FA / RA and carries C0 serve xi_z then p, FB / RB and C1 serve v_x then v_z.
-template <int CW, int R, int NX, int NZ>
-__global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band5_kernel(StepArgs<float> a, BandDev bd)
-{
-    extern __shared__ __align__(16) float smb[];
-    const int nz = NZ ? NZ : a.nz, nx = NX ? NX : a.nx;
-    const int G = blockDim.x / CW;
-    const int ncar = 2 * G * CW + BandCarry<CW, R>::floats_fixed();
-    float *FA = smb;
-    float *FB = FA + (size_t)nz * CW;
-    float *RA = FB + (size_t)nz * CW;
-    float *RB = RA + (size_t)nz * CW;
-    const BandCarry<CW, R> C0(RB + (size_t)nz * CW, G), C1(RB + (size_t)nz * CW + ncar, G);
-    float *KPB = RB + (size_t)nz * CW + 2 * ncar;
-    float *Kst = KPB, *Kri = KPB + nz, *Kr0 = KPB + 2 * nz, *Kgp = KPB + 3 * nz, *Kgr = KPB + 4 * nz, *Kg = KPB + 5 * nz,
-          *Kc2 = KPB + 6 * nz;
-    for (int k = threadIdx.x; k < nz; k += blockDim.x) {  // depth profiles
-        Kst[k] = __ldg(a.stretch + k);
-        Kri[k] = __ldg(a.rhoinv + k);
-        Kr0[k] = __ldg(a.rho0 + k);
-        Kgp[k] = __ldg(a.gp0 + k);
-        Kgr[k] = __ldg(a.gr0 + k);
-        Kg[k] = __ldg(a.g + k);
-        Kc2[k] = a.c2d ? 0.f : __ldg(a.c2rho0 + k);
-    }
-    const int c = threadIdx.x % CW, g = threadIdx.x / CW;
-    const int x = blockIdx.x * CW + c;
-    const int b = blockIdx.y;
-    const int k0 = g * R;
-    const int n = (NZ && NZ % R == 0) ? R : min(R, nz - k0);
-    const size_t F = (size_t)nz * nx;
-    const float *Ab = a.A + (size_t)b * 4 * F;
-    const int s = a.stage;
-    const float bs = a.bs, bsm1 = a.bsm1;
-    const int time = *a.d_time;
-    const bool flows = a.flows;
-    const bool xbc = (x == 0 || x == nx - 1);
-    // does this thread group hold vertical-PML rows (uniform over the group: a warp for CW = 32)
-    const bool pml_group = k0 < a.npmlbot || k0 + n > nz - a.npmltop;
-
-    // L2 prefetch of the per-point inputs of phases 3 and 5 for this thread group's rows
-    if constexpr (CW == 32) {
-        const size_t ob = (size_t)k0 * nx + (size_t)blockIdx.x * CW;  // row k0, first column
-        for (int i = c; i < 6 * R; i += CW) {
-            const int ai = i / R, m = i - ai * R;
-            if (m >= n) continue;
-            const float *p;
-            switch (ai) {
-                case 0: p = a.DX + (size_t)b * F; break;
-                case 1: p = flows ? a.FXX + (size_t)b * F : nullptr; break;
-                case 2: p = s >= 2 ? svp(a, a.slot_sm1, b, 1) : nullptr; break;
-                case 3: p = flows ? a.FXZ + (size_t)b * F : nullptr; break;
-                case 4: p = a.c2d ? a.c2rho0 + (size_t)b * a.bg2 : nullptr; break;
-                default: p = flows ? a.v0z + (size_t)b * a.bg2 : nullptr; break;
-            }
-            if (p) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + ob + (size_t)m * nx) : "memory");
-        }
-    }
-
-    // ---- 1: xi_z at stage s (scr xi_z = v_z of stage s-1 with the RHS boundary zeros) and v_x
-    float xz[R];
+    float *svz = svp(a, a.slot_s, b, 1);
 #pragma unroll
     for (int m = 0; m < R; m++) {
-        xz[m] = 0.f;
         if (m < n) {
             const int k = k0 + m;
             const size_t q = (size_t)k * nx + x;
-            float v = __ldg(Ab + F_XIZ * F + q);
-            if (s >= 2) {
-                const float avz = __ldg(Ab + F_VZ * F + q);
-                float t = (s == 2) ? avz : avz + bsm1 * __ldg(svp(a, a.slot_sm2, b, 1) + q);
-                if (k == 0 || xbc) t = 0.f;
-                v += bs * t;
-            }
-            xz[m] = v;
-            FA[k * CW + c] = v;
-            if (flows) {
-                float vx = __ldg(Ab + F_VX * F + q);
-                if (s >= 2) vx += bs * __ldg(svp(a, a.slot_sm1, b, 0) + q);
-                FB[k * CW + c] = vx;
-            }
+            svz[q] = xz[m];
+            a.RVXP[(size_t)b * F + q] = FB[k * CW + c];
         }
     }
-    __syncthreads();
-    // ---- 2: right-hand sides of d xi_z/dz (ibc 3, top value -dxi_x/dx * unstretch) and dv_x/dz (ibc 1)
-    {
-        float ra[R];
-        const float preset3 = -__ldg(a.TOPDX + (size_t)b * nx + x) * a.unstretch_top;
-        band_rhs<CW, R>(a.z3, FA, RA, c, k0, n, nz, preset3, ra);
-        band_publish<CW, R>(bd, bd.uv[2], C0, c, g, k0, n, nz, ra);
-    }
-    if (flows) {
-        float rr[R];
-        band_rhs<CW, R>(a.z1, FB, RB, c, k0, n, nz, 0.f, rr);
-        band_publish<CW, R>(bd, bd.uv[0], C1, c, g, k0, n, nz, rr);
-    }
-    __syncthreads();
-    // ---- 3: d xi_z/dz, vertical PML, divergence, pressure; advection of v_x along z; v_z of stage s
-    {
-        float d[R];
-        band_eval<CW, R>(bd, bd.uv[2], C0, c, g, G, k0, n, nz, RA, d);
+    if (pml_group) {
 #pragma unroll
         for (int m = 0; m < R; m++) {
-            if (m < n) {
-                const int k = k0 + m;
-                const size_t q = (size_t)k * nx + x;
-                float dzz = d[m] * Kst[k];
-                const int pi = pml_group ? pml_row(a, k) : -1;
-                float fd = 1.f;
-                if (pi >= 0) {
-                    const size_t qz = ((size_t)b * 2 * a.nzpml + pi) * nx + x;  // psi_vz
-                    const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
-                    float ps = __ldg(a.PZ + qz);
-                    if (s >= 2) ps += bs * __ldg(a.SPZ + (size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz);
-                    a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz] =
-                        __ldg(a.az + qb) * dzz + __ldg(a.bz + qb) * ps;
-                    dzz += ps;
-                    fd = __ldg(a.fdz + qb);
-                }
-                const float div = __ldg(a.DX + (size_t)b * F + q) + dzz;
-                const float c2r = a.c2d ? __ldg(a.c2rho0 + (size_t)b * a.bg2 + q) : Kc2[k];
-                const float gp = Kgp[k] * fd, gr = Kgr[k] * fd;
-                const float p = -c2r * div - gp * xz[m];
-                const float rho = -Kr0[k] * div - gr * xz[m];
-                xz[m] = rho * Kg[k];
-                FA[k * CW + c] = p;
-                a.P[(size_t)b * F + q] = p;
-            }
-        }
-        if (flows) band_eval<CW, R>(bd, bd.uv[0], C1, c, g, G, k0, n, nz, RB, d, true);
-#pragma unroll
-        for (int m = 0; m < R; m++) {
-            if (m < n) {
-                const int k = k0 + m;
-                const size_t q = (size_t)k * nx + x;
-                float rv = 0.f;
-                if (flows) {
-                    const float dvxdz = d[m] * Kst[k];
-                    rv = __ldg(a.FXX + (size_t)b * F + q) -
-                         2.f * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvxdz;
-                    float vz = __ldg(Ab + F_VZ * F + q);
-                    if (s >= 2) vz += bs * __ldg(svp(a, a.slot_sm1, b, 1) + q);
-                    FB[k * CW + c] = vz;
-                }
-                a.RVXP[(size_t)b * F + q] = rv;
-            }
-        }
-    }
-    __syncthreads();
-    // ---- 4: right-hand sides of dp/dz (ibc 2, bottom value 0) and dv_z/dz (ibc 1)
-    {
-        float rr[R];
-        band_rhs<CW, R>(a.z2, FA, RA, c, k0, n, nz, 0.f, rr);
-        band_publish<CW, R>(bd, bd.uv[1], C0, c, g, k0, n, nz, rr);
-    }
-    if (flows) {
-        float rr[R];
-        band_rhs<CW, R>(a.z1, FB, RB, c, k0, n, nz, 0.f, rr);
-        band_publish<CW, R>(bd, bd.uv[0], C1, c, g, k0, n, nz, rr);
-    }
-    __syncthreads();
-    // ---- 5: gradient of p and RHS v_z (buoyancy, advection, source, boundary zeros)
-    float forcing = 0.f;
-    const bool inject = (time <= a.src_until) && (time >= 0) && (time < a.ntab);
-    if (inject && a.k_inj >= k0 && a.k_inj < k0 + n) {
-        const double *w = a.src_w + (size_t)time * 7;
-        const int i0 = a.src_idx[time];
-        double f = 0.0;
-        for (int jj = 0; jj < 7; jj++) {
-            const int r = i0 + jj;
-            if (r >= 0 && r < a.nrows && w[jj] != 0.0)
-                f += w[jj] * (double)__ldg(a.src_rows + ((size_t)b * a.nrows + r) * nx + x);
-        }
-        forcing = (float)f * __ldg(a.inj_scale + (size_t)b * nx + x);
-    }
-    {
-        float d[R];
-        band_eval<CW, R>(bd, bd.uv[1], C0, c, g, G, k0, n, nz, RA, d, true);
-#pragma unroll
-        for (int m = 0; m < R; m++) {
-            if (m < n) {
-                const int k = k0 + m;
-                float gpz = d[m] * Kst[k];
-                const int pi = pml_group ? pml_row(a, k) : -1;
-                if (pi >= 0) {
-                    const size_t qz = (((size_t)b * 2 + 1) * a.nzpml + pi) * nx + x;  // psi_p
-                    const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
-                    float ps = __ldg(a.PZ + qz);
-                    if (s >= 2) ps += bs * __ldg(a.SPZ + (size_t)a.slot_sm1 * a.nb * 2 * a.nzpml * nx + qz);
-                    a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz] =
-                        __ldg(a.az + qb) * gpz + __ldg(a.bz + qb) * ps;
-                    gpz += ps;
-                }
-                xz[m] = -Kri[k] * (gpz + xz[m]);
-            }
-        }
-        if (flows) band_eval<CW, R>(bd, bd.uv[0], C1, c, g, G, k0, n, nz, RB, d, true);
-        float *svz = svp(a, a.slot_s, b, 1);
-#pragma unroll
-        for (int m = 0; m < R; m++) {
-            if (m < n) {
-                const int k = k0 + m;
-                const size_t q = (size_t)k * nx + x;
-                float r = xz[m];
-                if (k == a.k_inj) r += forcing;
-                if (flows) {
-                    const float dvzdz = d[m] * Kst[k];
-                    r += __ldg(a.FXZ + (size_t)b * F + q) -
-                         2.f * a.fsign * __ldg(a.v0z + (size_t)b * a.bg2 + q) * dvzdz;
-                }
-                if (k == 0 || xbc) r = 0.f;
-                svz[q] = r;
+            const int pi = m < n ? pml_row(a, k0 + m) : -1;
+            if (pi >= 0) {
+                const size_t qz = ((size_t)b * 2 * nzp + pi) * nx + x;
+                a.SPZ[a.slot_s * spz_slot + qz] = PS[(0 * nzp + pi) * CW + c];
+                a.SPZ[a.slot_s * spz_slot + qz + (size_t)nzp * nx] = PS[(1 * nzp + pi) * CW + c];
             }
         }
     }
@@ -466,24 +295,25 @@ int col_band_rows(int nz, int cw)
 }
 
 template <int CW, int R>
-static size_t band_smem(int nz)
+static size_t band_smem(int nz, int nzpml)
 {
     const int G = (nz + R - 1) / R;
-    return ((size_t)4 * nz * CW + 2 * ((size_t)2 * G * CW + BandCarry<CW, R>::floats_fixed()) + (size_t)7 * nz) * sizeof(float);
+    return ((size_t)4 * nz * CW + 2 * ((size_t)2 * G * CW + BandCarry<CW, R>::floats_fixed()) + (size_t)7 * nz +
+            (size_t)5 * nzpml * CW) * sizeof(float);
 }
 
-size_t col_band_smem_bytes(int nz, int R, int cw)
+size_t col_band_smem_bytes(int nz, int nzpml, int R, int cw)
 {
     switch (cw * 100 + R) {
-        case 3208: return band_smem<32, 8>(nz);
-        case 3210: return band_smem<32, 10>(nz);
-        case 3212: return band_smem<32, 12>(nz);
-        case 1609: return band_smem<16, 9>(nz);
-        case 1611: return band_smem<16, 11>(nz);
-        case 1613: return band_smem<16, 13>(nz);
-        case 809: return band_smem<8, 9>(nz);
-        case 811: return band_smem<8, 11>(nz);
-        case 813: return band_smem<8, 13>(nz);
+        case 3208: return band_smem<32, 8>(nz, nzpml);
+        case 3210: return band_smem<32, 10>(nz, nzpml);
+        case 3212: return band_smem<32, 12>(nz, nzpml);
+        case 1609: return band_smem<16, 9>(nz, nzpml);
+        case 1611: return band_smem<16, 11>(nz, nzpml);
+        case 1613: return band_smem<16, 13>(nz, nzpml);
+        case 809: return band_smem<8, 9>(nz, nzpml);
+        case 811: return band_smem<8, 11>(nz, nzpml);
+        case 813: return band_smem<8, 13>(nz, nzpml);
         default: return ~(size_t)0;
     }
 }
@@ -494,12 +324,12 @@ static cudaError_t launch_band(const StepArgs<float> &a, const BandDev &bd, cuda
     const int G = (a.nz + R - 1) / R;
     if (G > band_maxg<CW>() || a.nx % CW != 0 || R * G - a.nz >= R) return cudaErrorInvalidValue;
     if ((NX && a.nx != NX) || (NZ && a.nz != NZ)) return cudaErrorInvalidValue;
-    const size_t smem = band_smem<CW, R>(a.nz);
-    auto kern = a.band_phases == 7 ? col_band_kernel<CW, R, NX, NZ> : col_band5_kernel<CW, R, NX, NZ>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = band_smem<CW, R>(a.nz, a.nzpml);
+    cudaError_t e = cudaFuncSetAttribute(col_band_kernel<CW, R, NX, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid(a.nx / CW, a.nb);
-    kern<<<grid, G * CW, smem, st>>>(a, bd);
+    col_band_kernel<CW, R, NX, NZ><<<grid, G * CW, smem, st>>>(a, bd);
     return cudaGetLastError();
 }
 

@@ -63,7 +63,6 @@ struct StepArgs {
     int src_until, k_inj, k_obs, steps_out;
     int filt_k0, filt_xall;  // FILTER_VARS_2D coverage (rows from filt_k0, all columns if filt_xall)
     int colw;                // column-pass block width (8 or 32 columns)
-    int band_phases;         // banded column pass: 5 (two derivatives per phase) or 7 phases
     int boxr;                // rows per TMA box of the staged column pass (2 boxes cover nz)
     int *d_err;              // device error flag (SPARC_DEV_ERR_*)
     const T *inj_scale, *src_rows;
@@ -467,7 +466,7 @@ cudaError_t launch_s5_axpy(long long n, T *Y, const T *X, T a, cudaStream_t st);
 
 template <int CW, int R>
 cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st);
-size_t col_band_smem_bytes(int nz, int R, int cw);
+size_t col_band_smem_bytes(int nz, int nzpml, int R, int cw);
 bool col_band_specialised(int nx, int nz, int cw, int R);  // compiled for this grid
 int col_band_rows(int nz, int cw);  // rows per thread group (0: no banded pass for this depth / width)
 

@@ -49,7 +49,31 @@ __global__ void __launch_bounds__(END_CW *END_WARPS) end_step_stream_kernel(Step
     const T dt = a.dt, bs = a.bs;
     const bool xbc = (x == 0 || x == nx - 1);
 
-    // ---- 1: updated fields into shared memory; psi component p of the vertical PML; acc record
+    // ---- 0: psi component p of the vertical PML, pmlvars += deltat * scrpml (step.f90:112-115):
+    // the thread's PML rows (w, w + 16, ... within the bottom and top layers), all loads first
+    {
+        constexpr int MP = 4;  // PML rows per batch and thread (the PML arrays hold both layers)
+        const size_t ring = (size_t)a.slot_s * a.nb * 2 * a.nzpml * nx;
+        for (int base = w; base < a.nzpml; base += MP * END_WARPS) {
+            T pv[MP];
+            size_t qv[MP];
+            int np = 0;
+#pragma unroll
+            for (int i = 0; i < MP; i++) {
+                const int pi = base + i * END_WARPS;
+                if (pi < a.nzpml) {
+                    const size_t qz = (((size_t)b * 2 + p) * a.nzpml + pi) * nx + x;
+                    qv[i] = qz;
+                    pv[i] = a.PZ[qz] + dt * a.SPZ[ring + qz];
+                    np = i + 1;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < MP; i++)
+                if (i < np) a.PZ[qv[i]] = pv[i];
+        }
+    }
+    // ---- 1: updated fields into shared memory; acc record
 #pragma unroll 4
     for (int k = w; k < nz; k += END_WARPS) {
         const size_t g = (size_t)k * nx + x;
@@ -58,11 +82,6 @@ __global__ void __launch_bounds__(END_CW *END_WARPS) end_step_stream_kernel(Step
         Uxi[k * END_CW + c] = xi + dt * sxi;
         Uv[k * END_CW + c] = v + dt * r5;
         if (snap) snap[(size_t)(4 + p) * F + g] = r5;
-        const int pi = pml_row(a, k);
-        if (pi >= 0) {  // pmlvars += deltat * scrpml (step.f90:112-115)
-            const size_t qz = (((size_t)b * 2 + p) * a.nzpml + pi) * nx + x;
-            a.PZ[qz] += dt * a.SPZ[(size_t)a.slot_s * a.nb * 2 * a.nzpml * nx + qz];
-        }
     }
     __syncthreads();
     // ---- 2: FILTER_VARS_2D, state in place, records

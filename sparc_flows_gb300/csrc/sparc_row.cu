@@ -176,10 +176,82 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
     for (int x = lane; x < N; x += WARP) row_out(a, r, x, o2r[x] * isr2, o2i[x] * isi2);
 }
 
-// FP32 rows of 512 columns: the same row pass with the register-resident FFT (sparc_fft512.cuh);
-// register n2 of a lane holds column lane + 32 n2.
+// row_mid without global stores, for the register-FFT pass: the loads and arithmetic of column x;
+// what row_mid stores is returned (svx: RHS v_x of stage s-1, dxo: dxi_x/dx) or, for the x-PML
+// columns, left in the warp scratch P ([3][nhx]: psi_vx RHS or, closing pass, the new psi_vx;
+// psi_gradp_x RHS; closing pass, the new psi_gradp_x).  The stores follow in row_mid_store.
 template <int MODE>
-__global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_reg512_kernel(StepArgs<float> a)
+__device__ __forceinline__ void row_mid_load(const StepArgs<float> &a, const RowCtx<float> &r, int x, float gpx,
+                                             float dxx, float *P, float &svx, float &dxo, float &vxs, float &vzs)
+{
+    const int b = r.b, k = r.k, nx = r.nx, nh = r.nh, nhx = r.nhx;
+    const size_t F = r.F, ro = r.ro;
+    const bool pml = (x < nh) || (x >= nx - nh);
+    const int ai = (x < nh) ? x : x - (nx - nh) + nh;
+    if (pml) {
+        const float axv = __ldg(r.axk + ai), bxv = __ldg(r.bxk + ai);
+        float ngp = 0.f;
+        if (MODE != 0) {  // psi_gradp_x of stage s-1
+            const size_t q = ((size_t)1 * a.nz + k) * nhx + ai;
+            float ps = r.PXb[q];
+            if (a.stage >= 3) ps += r.bsm1 * a.SPX[((size_t)a.slot_sm2 * a.nb + b) * 2 * a.nz * nhx + q];
+            gpx += ps;
+            ngp = axv * gpx + bxv * ps;
+            P[nhx + ai] = ngp;
+        }
+        if (MODE != 2) {  // psi_vx of stage s
+            const size_t q = ((size_t)0 * a.nz + k) * nhx + ai;
+            float ps = r.PXb[q];
+            if (MODE == 1) ps += r.bs * a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q];
+            dxx += ps;
+            P[ai] = axv * dxx + bxv * ps;
+        } else {  // closing pass: pmlvarsx += deltat * scrpmlx (step.f90:112-115)
+            const size_t q0 = ((size_t)0 * a.nz + k) * nhx + ai, q1 = ((size_t)1 * a.nz + k) * nhx + ai;
+            P[ai] = r.PXb[q0] + a.dt * a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q0];
+            P[2 * nhx + ai] = r.PXb[q1] + a.dt * ngp;
+        }
+    }
+    svx = 0.f;
+    if (MODE != 0) {
+        svx = __ldg(a.RVXP + (size_t)b * F + ro + x) - r.rhoinv_k * gpx;
+        if (k == 0 || x == 0 || x == nx - 1) svx = 0.f;
+    }
+    dxo = dxx;
+    vxs = 0.f;
+    vzs = 0.f;
+    if (MODE != 2) {
+        vxs = __ldg(r.Ab + F_VX * F + ro + x);
+        vzs = __ldg(r.Ab + F_VZ * F + ro + x);
+        if (MODE == 1) {
+            vxs += r.bs * svx;
+            vzs += r.bs * __ldg(svp(a, a.slot_sm1, b, 1) + ro + x);
+        }
+    }
+}
+
+// The x-PML stores of row_mid_load from the warp scratch P (lanes over the PML columns).
+template <int MODE>
+__device__ __forceinline__ void row_mid_store_pml(const StepArgs<float> &a, const RowCtx<float> &r, const float *P,
+                                                  int lane)
+{
+    const int b = r.b, k = r.k, nhx = r.nhx;
+    for (int ai = lane; ai < nhx; ai += WARP) {
+        const size_t q0 = ((size_t)0 * a.nz + k) * nhx + ai, q1 = ((size_t)1 * a.nz + k) * nhx + ai;
+        if (MODE != 0) a.SPX[((size_t)a.slot_sm1 * a.nb + b) * 2 * a.nz * nhx + q1] = P[nhx + ai];
+        if (MODE != 2) {
+            a.SPX[((size_t)a.slot_s * a.nb + b) * 2 * a.nz * nhx + q0] = P[ai];
+        } else {
+            r.PXb[q0] = P[ai];
+            r.PXb[q1] = P[2 * nhx + ai];
+        }
+    }
+}
+
+// FP32 rows of 512 columns: the same row pass with the register-resident FFT (sparc_fft512.cuh);
+// register n2 of a lane holds column lane + 32 n2.  Each part loads everything it needs before it
+// stores anything, so no load waits behind a store of the row it may alias.
+template <int MODE>
+__global__ void __launch_bounds__(ROW_WPB *WARP, 4) row_stage_reg512_kernel(StepArgs<float> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -203,22 +275,46 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_reg512_kernel(StepArg
     fft512_deriv(re, im, S, a.twr, a.twi, a.kap, a.stretchx, lane, sr, si);
 
     float mr2 = 0.f, mi2 = 0.f;
+    float svx[16], dxo[16];
+    __syncwarp();  // the transform's last reads of S are done before S holds the x-PML values
 #pragma unroll
     for (int n2 = 0; n2 < 16; n2++) {
         float vxs, vzs;
-        row_mid<float, MODE>(a, r, lane + 32 * n2, re[n2] * isr, im[n2] * isi, vxs, vzs);
+        row_mid_load<MODE>(a, r, lane + 32 * n2, re[n2] * isr, im[n2] * isi, S, svx[n2], dxo[n2], vxs, vzs);
         re[n2] = vxs;
         im[n2] = vzs;
         mr2 = fmaxf(mr2, fabsf(vxs));
         mi2 = fmaxf(mi2, fabsf(vzs));
     }
+    __syncwarp();
+    row_mid_store_pml<MODE>(a, r, S, lane);
+    {
+        const size_t F = r.F, ro = r.ro;
+#pragma unroll
+        for (int n2 = 0; n2 < 16; n2++) {
+            const int x = lane + 32 * n2;
+            if (MODE != 0) svp(a, a.slot_sm1, r.b, 0)[ro + x] = svx[n2];
+            if (MODE != 2) {
+                a.DX[(size_t)r.b * F + ro + x] = dxo[n2];
+                if (r.k == a.nz - 1) a.TOPDX[(size_t)r.b * 512 + x] = dxo[n2];
+            }
+        }
+    }
     if (MODE == 2 || !a.flows) return;
+    __syncwarp();  // the x-PML values are read before the next transform reuses S
     float sr2, si2, isr2, isi2;
     warp_row_scale(mr2, sr2, isr2);
     warp_row_scale(mi2, si2, isi2);
     fft512_deriv(re, im, S, a.twr, a.twi, a.kap, a.stretchx, lane, sr2, si2);
+    float wv[16];  // -2 v0x of the row, loaded before the advection terms are stored
 #pragma unroll
-    for (int n2 = 0; n2 < 16; n2++) row_out(a, r, lane + 32 * n2, re[n2] * isr2, im[n2] * isi2);
+    for (int n2 = 0; n2 < 16; n2++) wv[n2] = -2.f * a.fsign * __ldg(a.v0x + (size_t)r.b * a.bg2 + r.ro + lane + 32 * n2);
+#pragma unroll
+    for (int n2 = 0; n2 < 16; n2++) {
+        const size_t q = (size_t)r.b * r.F + r.ro + lane + 32 * n2;
+        a.FXX[q] = wv[n2] * (re[n2] * isr2);
+        a.FXZ[q] = wv[n2] * (im[n2] * isi2);
+    }
 }
 
 // Generic spectral x-derivative of nrows rows (two rows per warp).
