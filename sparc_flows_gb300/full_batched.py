@@ -17,6 +17,14 @@ kernel/{kernel_c, kernel_vx, kernel_vz, kernel_psi, hessian}_NN.fits are written
 No partial states touch the disk.  Environment as the sparc drop-in: SPARC_PRECISION,
 SPARC_DEVICE, SPARC_NSTEPS, SPARC_ADJOINT_SOURCE; SPARC_CHECKPOINT_EVERY=K keeps checkpoints
 every K records instead of all partial states.
+
+Several GPUs: launched under torchrun (RANK, WORLD_SIZE, LOCAL_RANK and MASTER_* in the
+environment), every rank takes its contiguous share of the sources (distributed.shard; the
+reference runs one sparc process per source, full.py:85-93), runs it on cuda:LOCAL_RANK and writes
+that share's files; the kernel sums grad.py forms over all sources (grad.py:188-196: the sum of
+kernel_psi and of |hessian|) are then one all-reduce (distributed.sum_kernels), and rank 0 writes
+them to kernel/kernel_psi_sum.fits and kernel/hessian_sum.fits (no reference counterpart: grad.py
+re-reads the per-source files, which are all written as before).
 """
 from __future__ import annotations
 
@@ -28,10 +36,14 @@ import numpy as np
 
 from . import cli, fits
 from .config import parse_params_i, run_config_from_params
+from .distributed import shard, sum_kernels
 from .model import SPATIAL_REFERENCE, TEMPORAL_REFERENCE, SourceSpec, load_model
 
 
-def run_iteration(sources: list[int] | None = None, jobno: str = "00") -> int:
+def run_iteration(sources: list[int] | None = None, jobno: str = "00", rank: int = 0, world: int = 1) -> dict:
+    """Forward, adjoint and kernel stages of this rank's share of the sources; returns the kernel
+    sums over every source of every rank ({"kernel_psi", "hessian"}: sum of kernel_psi and of
+    |hessian|, (nz, nx) FP64, on every rank)."""
     import torch
 
     from .pipeline import FwdAdjKernels
@@ -42,12 +54,15 @@ def run_iteration(sources: list[int] | None = None, jobno: str = "00") -> int:
     if os.environ.get("SPARC_NSTEPS"):
         run = run.replace(nsteps=int(os.environ["SPARC_NSTEPS"]))
     precision = int(os.environ.get("SPARC_PRECISION", "64"))
-    device = os.environ.get("SPARC_DEVICE", "cuda:0")
+    device = os.environ.get("SPARC_DEVICE", f"cuda:{int(os.environ.get('LOCAL_RANK', '0'))}")
     ck = int(os.environ.get("SPARC_CHECKPOINT_EVERY", "0")) or None
     model = load_model(params.get("file_data", "solar_deep"), run.nz)
     with open(os.path.join(directory, "master.pixels")) as f:
         npix = len([ln for ln in f if ln.strip()])
-    sources = sources or list(range(1, min(npix, 100) + 1))
+    sources = shard(sources or list(range(1, min(npix, 100) + 1)), rank, world)
+    partial = {k: torch.zeros((run.nz, run.nx), dtype=torch.float64) for k in ("kernel_psi", "hessian")}
+    if not sources:  # more ranks than sources: this rank only joins the kernel sum
+        return _sum_and_write(partial, directory, rank)
     contribs = [f"{s:02d}" for s in sources]
     xlocs = [cli._master_pixel(directory, s) for s in sources]
     psi, direct = cli._flow_inputs(run, directory, jobno, False)
@@ -70,7 +85,25 @@ def run_iteration(sources: list[int] | None = None, jobno: str = "00") -> int:
         cli._write_kernel_files(directory, contrib, {k: v[b] for k, v in ker.items()})
         cli._write_adjoint_info(os.path.join(directory, f"adjoint_src{contrib}"), run)
     pipe.close()
-    return 0
+    partial["kernel_psi"] += torch.as_tensor(ker["kernel_psi"]).sum(0)
+    partial["hessian"] += torch.as_tensor(ker["hessian"]).abs().sum(0)
+    return _sum_and_write(partial, directory, rank)
+
+
+def _sum_and_write(partial: dict, directory: str, rank: int) -> dict:
+    """The kernel sums over all ranks (grad.py:188-196); rank 0 writes them."""
+    import torch
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized() and dist.get_backend() == "nccl":
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        partial = {k: v.to(dev) for k, v in partial.items()}
+    tot = sum_kernels(partial)
+    if rank == 0:
+        os.makedirs(os.path.join(directory, "kernel"), exist_ok=True)
+        for name in ("kernel_psi", "hessian"):
+            fits.write(os.path.join(directory, "kernel", f"{name}_sum.fits"), tot[name].cpu().numpy()[:, None, :])
+    return tot
 
 
 def main(argv=None) -> int:
@@ -79,7 +112,18 @@ def main(argv=None) -> int:
     ap.add_argument("--jobno", default="00")
     a = ap.parse_args(argv)
     srcs = [int(v) for v in a.sources.split(",") if v.strip()] or None
-    return run_iteration(srcs, a.jobno)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo" if os.environ.get("SPARC_DIST_BACKEND") == "gloo" else "nccl")
+    try:
+        run_iteration(srcs, a.jobno, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+    return 0
 
 
 if __name__ == "__main__":
