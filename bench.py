@@ -546,6 +546,14 @@ def run_uneven(args):
                            "column_pass_autotuned": {f"{k[0]}x{k[1]}": list(v["choice"]) for k, v in ub.tuned.items()},
                            "l2": "inputs larger than L2", "parallelism": "9 batched plans on 9 concurrent streams"},
                 "clocks": clk.summary(), "gpu_launches": None}
+        if args.accuracy:
+            errs = ub.errors_against_fp64()
+            names = [k for k in errs[0] if k not in ("nx", "nsteps")]
+            line["per_solve_error_vs_fp64"] = {
+                "solves": [{"nx": e["nx"], "nsteps": e["nsteps"], **{k: e[k] for k in names}} for e in errs],
+                "max": {k: max(e[k] for e in errs) for k in names},
+                "how": "rel-L2 of each solve's FP32 seismograms and scaled kernels against the same solve "
+                       "run through FP64 plans"}
         print(json.dumps(line), flush=True)
     ub.close()
 
@@ -630,6 +638,8 @@ def main():
     ap.add_argument("--no-gradient", action="store_true", help="skip the gradient post-processing figures")
     ap.add_argument("--no-checkpoint", action="store_true", help="skip the checkpointed-run figures")
     ap.add_argument("--autotune", action="store_true", help="uneven48: time column-pass variants per group first")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="uneven48: each solve's FP32 error against the same solve in FP64 (one more FP64 run)")
     ap.add_argument("--workload", default="batch32", choices=["batch32", "uneven48", "3d4"],
                     help="uneven48: 48 solves of mixed grids, lengths and backgrounds (seed 0)")
     args = ap.parse_args()

@@ -20,6 +20,11 @@ from . import model as M
 from .pipeline import FwdAdjKernels, receiver_columns
 
 
+def _rel(a: torch.Tensor, b: torch.Tensor) -> float:
+    a, b = a.double(), b.double()
+    return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b).clamp_min(1e-300))
+
+
 def group_solves(solves: list) -> dict:
     """{(nx, nsteps): [indices into solves]}"""
     groups: dict = {}
@@ -60,7 +65,7 @@ class UnevenBatch:
         self.solves, self.dev = solves, torch.device(device)
         model = M.polytrope(300)
         self.groups = group_solves(solves)
-        self.pipes, self.streams, self.tuned = {}, {}, {}
+        self.pipes, self.streams, self.tuned, self._inputs = {}, {}, {}, {}
         for key, idx in self.groups.items():
             nx, nsteps = key
             run = M.uneven_run(nx, nsteps)
@@ -80,6 +85,7 @@ class UnevenBatch:
             self.pipes[key] = FwdAdjKernels(run, model, specs, psi=psis, cmul=cmuls, precision=precision,
                                             receivers=rcv, device=device, **col)
             self.streams[key] = torch.cuda.Stream(device=self.dev)
+            self._inputs[key] = (run, model, specs, psis, cmuls, rcv)
 
     def point_steps(self) -> int:
         """Useful grid-point steps of one run (forward and adjoint counted once each)."""
@@ -104,6 +110,28 @@ class UnevenBatch:
             t.join()
         if errors:
             raise RuntimeError(f"uneven batch group {errors[0][0]} failed: {errors[0][1]}")
+
+    def errors_against_fp64(self) -> list[dict]:
+        """Relative L2 error of every solve's seismograms and scaled kernels from the last run()
+        against the same solve in FP64 (the same inputs through FP64 plans, one group at a time);
+        one dict per solve, in the order of the solves."""
+        out: list = [None] * len(self.solves)
+        for key, idx in self.groups.items():
+            run, model, specs, psis, cmuls, rcv = self._inputs[key]
+            p32 = self.pipes[key]
+            p64 = FwdAdjKernels(run, model, specs, psi=psis, cmul=cmuls, precision=64, receivers=rcv,
+                                device=str(self.dev))
+            with torch.cuda.device(self.dev):
+                p64.run_all()
+                torch.cuda.synchronize()
+                k32, k64 = p32.final_kernels(summed=False), p64.final_kernels(summed=False)
+                for j, i in enumerate(idx):
+                    e = {"nx": run.nx, "nsteps": run.nsteps,
+                         "seismograms": _rel(p32.seis[j], p64.seis[j])}
+                    e.update({name: _rel(k32[name][j], k64[name][j]) for name in k64})
+                    out[i] = e
+            p64.close()
+        return out
 
     def seismograms(self, i: int) -> torch.Tensor:
         """Seismograms (nrec, nx) of solve i from the last run."""
