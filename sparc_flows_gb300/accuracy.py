@@ -42,6 +42,10 @@ def fp32_vs_fp64(workload: str = "batch32", source: int = 15, nsteps: int | None
     for name in k64:
         rep[name] = rel_l2(k32[name], k64[name])
     rep["max"] = max(v for k, v in rep.items() if k not in ("workload", "source_x_mm", "nsteps"))
+    # the metric's condition: every seismogram and kernel within 1e-4 rel-L2 of FP64
+    rep["bound"] = 1e-4
+    rep["within_bound"] = {k: bool(rep[k] <= 1e-4) for k in ["seismograms", *k64]}
+    rep["pass"] = all(rep["within_bound"].values())
     # the same over the physical interior: rows and columns of the absorbing layers left out
     zs = slice(run.npmlbot, run.nz - run.npmltop)
     xs = slice(run.npmlhor, run.nx - run.npmlhor)

@@ -61,26 +61,24 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     // computes into registers or shared memory, and stores last), so that the loads of one row
     // never queue behind a possibly aliasing store of the previous row.
 
-    // ---- 0: PML inputs of the thread's own rows into shared memory (only the thread reads them)
-    if (pml_group) {
-#pragma unroll
-        for (int m = 0; m < R; m++) {
-            const int pi = m < n ? pml_row(a, k0 + m) : -1;
-            if (pi >= 0) {
-                const size_t qz = ((size_t)b * 2 * nzp + pi) * nx + x;  // psi_vz; psi_p at + nzp * nx
-                const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + x;
-                float p0 = __ldg(a.PZ + qz), p1 = __ldg(a.PZ + qz + (size_t)nzp * nx);
-                if (s >= 2) {
-                    p0 += bs * __ldg(a.SPZ + a.slot_sm1 * spz_slot + qz);
-                    p1 += bs * __ldg(a.SPZ + a.slot_sm1 * spz_slot + qz + (size_t)nzp * nx);
-                }
-                PS[(0 * nzp + pi) * CW + c] = p0;
-                PS[(1 * nzp + pi) * CW + c] = p1;
-                PS[(2 * nzp + pi) * CW + c] = __ldg(a.az + qb);
-                PS[(3 * nzp + pi) * CW + c] = __ldg(a.bz + qb);
-                PS[(4 * nzp + pi) * CW + c] = __ldg(a.fdz + qb);
-            }
+    // ---- 0: PML inputs of the block's PML rows into shared memory, loads shared by all threads
+    // (the PML thread groups alone would each load seven values per row and hold every other
+    // group at the first barrier)
+    for (int i = threadIdx.x; i < nzp * CW; i += blockDim.x) {
+        const int pi = i / CW, cc = i - pi * CW;
+        const int xx = blockIdx.x * CW + cc;
+        const size_t qz = ((size_t)b * 2 * nzp + pi) * nx + xx;  // psi_vz; psi_p at + nzp * nx
+        const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + xx;
+        float p0 = __ldg(a.PZ + qz), p1 = __ldg(a.PZ + qz + (size_t)nzp * nx);
+        if (s >= 2) {
+            p0 += bs * __ldg(a.SPZ + a.slot_sm1 * spz_slot + qz);
+            p1 += bs * __ldg(a.SPZ + a.slot_sm1 * spz_slot + qz + (size_t)nzp * nx);
         }
+        PS[(0 * nzp + pi) * CW + cc] = p0;
+        PS[(1 * nzp + pi) * CW + cc] = p1;
+        PS[(2 * nzp + pi) * CW + cc] = __ldg(a.az + qb);
+        PS[(3 * nzp + pi) * CW + cc] = __ldg(a.bz + qb);
+        PS[(4 * nzp + pi) * CW + cc] = __ldg(a.fdz + qb);
     }
 
     // L2 prefetch of the later phases' per-point inputs of this thread group's rows: one
@@ -180,6 +178,10 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
 #pragma unroll
     for (int m = 0; m < R; m++)
         if (m < n) a.P[(size_t)b * F + (size_t)(k0 + m) * nx + x] = FA[(k0 + m) * CW + c];
+    for (int i = threadIdx.x; i < nzp * CW; i += blockDim.x) {  // new RHS of psi_vz (phase 3)
+        const int pi = i / CW, cc = i - pi * CW;
+        a.SPZ[a.slot_s * spz_slot + ((size_t)b * 2 * nzp + pi) * nx + blockIdx.x * CW + cc] = PS[(0 * nzp + pi) * CW + cc];
+    }
     __syncthreads();
     // ---- 5: gradient of p, RHS v_z without advection; advection of v_x along z (partial RHS
     // v_x kept in FB); v_z of stage s
@@ -268,16 +270,10 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
             a.RVXP[(size_t)b * F + q] = FB[k * CW + c];
         }
     }
-    if (pml_group) {
-#pragma unroll
-        for (int m = 0; m < R; m++) {
-            const int pi = m < n ? pml_row(a, k0 + m) : -1;
-            if (pi >= 0) {
-                const size_t qz = ((size_t)b * 2 * nzp + pi) * nx + x;
-                a.SPZ[a.slot_s * spz_slot + qz] = PS[(0 * nzp + pi) * CW + c];
-                a.SPZ[a.slot_s * spz_slot + qz + (size_t)nzp * nx] = PS[(1 * nzp + pi) * CW + c];
-            }
-        }
+    for (int i = threadIdx.x; i < nzp * CW; i += blockDim.x) {  // new RHS of psi_p (phase 5)
+        const int pi = i / CW, cc = i - pi * CW;
+        a.SPZ[a.slot_s * spz_slot + ((size_t)b * 2 * nzp + pi + nzp) * nx + blockIdx.x * CW + cc] =
+            PS[(1 * nzp + pi) * CW + cc];
     }
 }
 

@@ -43,7 +43,8 @@ def kernel_case():
     return run, model, psi, cmul, spec, rcv, seis_o, ker
 
 
-@pytest.mark.parametrize("precision,tol", [(64, 1e-9), (32, 2e-4)])
+# FP32: the metric's own bound, 1e-4 rel-L2 against the FP64 restatement
+@pytest.mark.parametrize("precision,tol", [(64, 1e-9), (32, 1e-4)])
 def test_kernels_match_oracle(kernel_case, precision, tol):
     from sparc_flows_gb300.pipeline import FwdAdjKernels
     run, model, psi, cmul, spec, rcv, seis_o, ker = kernel_case
@@ -52,6 +53,7 @@ def test_kernels_match_oracle(kernel_case, precision, tol):
     assert rel_l2(seis.cpu().numpy()[0], seis_o) < (1e-10 if precision == 64 else 1e-4)
     got = {k: v.cpu().numpy()[0] for k, v in pipe.final_kernels(summed=False).items()}
     pipe.close()
-    for name in ("kernel_c", "kernel_vx", "kernel_vz", "kernel_psi", "hessian"):
+    errs = {name: rel_l2(got[name], ker[name]) for name in ("kernel_c", "kernel_vx", "kernel_vz", "kernel_psi", "hessian")}
+    for name in errs:
         assert np.abs(ker[name]).max() > 0, name
-        assert rel_l2(got[name], ker[name]) < tol, (name, rel_l2(got[name], ker[name]))
+        assert errs[name] < tol, (name, errs)
