@@ -7,8 +7,6 @@
 // rows that are R apart; with R odd for CW < 32 they fall on disjoint banks.  Shared memory:
 // two field columns F[nz][CW], two right-hand-side columns [nz][CW], the carries of two
 // derivatives and seven depth profiles.
-#include <algorithm>
-
 #include "sparc_band.cuh"
 
 namespace sparc {
@@ -45,25 +43,19 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         Kc2[k] = a.c2d ? 0.f : __ldg(a.c2rho0 + k);
     }
     const int c = threadIdx.x % CW, g = threadIdx.x / CW;
+    const int x = blockIdx.x * CW + c;
+    const int b = blockIdx.y;
     const int k0 = g * R;
     const int n = (NZ && NZ % R == 0) ? R : min(R, nz - k0);
     const size_t F = (size_t)nz * nx;
+    const float *Ab = a.A + (size_t)b * 4 * F;
     const int s = a.stage;
     const float bs = a.bs, bsm1 = a.bsm1;
     const int time = *a.d_time;
+    const bool xbc = (x == 0 || x == nx - 1);
     // does this thread group hold vertical-PML rows (uniform over the group: a warp for CW = 32)
     const bool pml_group = k0 < a.npmlbot || k0 + n > nz - a.npmltop;
     const size_t spz_slot = (size_t)a.nb * 2 * nzp * nx;  // one slot of the PML RHS ring
-    const int tiles_x = nx / CW, ntiles = tiles_x * a.nb;
-
-    // Persistent: the block takes tiles (CW columns of one solve) blockIdx.x, + gridDim.x, ...;
-    // while one tile computes, the first-phase inputs of the block's next tile are prefetched to
-    // L2, so the loads that open a tile do not all wait on DRAM at once.
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int bx = tile % tiles_x, b = tile / tiles_x;
-    const int x = bx * CW + c;
-    const float *Ab = a.A + (size_t)b * 4 * F;
-    const bool xbc = (x == 0 || x == nx - 1);
 
     // Global stores wait until the loads of their phase are issued (every phase below loads,
     // computes into registers or shared memory, and stores last), so that the loads of one row
@@ -74,7 +66,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     // group at the first barrier)
     for (int i = threadIdx.x; i < nzp * CW; i += blockDim.x) {
         const int pi = i / CW, cc = i - pi * CW;
-        const int xx = bx * CW + cc;
+        const int xx = blockIdx.x * CW + cc;
         const size_t qz = ((size_t)b * 2 * nzp + pi) * nx + xx;  // psi_vz; psi_p at + nzp * nx
         const size_t qb = (size_t)b * a.bgz + (size_t)pi * nx + xx;
         float p0 = __ldg(a.PZ + qz), p1 = __ldg(a.PZ + qz + (size_t)nzp * nx);
@@ -93,7 +85,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     // 128-byte line per (array, row) for CW = 32, spread over the lanes, no registers held, so
     // those loads find their lines in L2 instead of waiting on DRAM phase by phase
     if constexpr (CW == 32) {
-        const size_t ob = (size_t)k0 * nx + (size_t)bx * CW;  // row k0, first column
+        const size_t ob = (size_t)k0 * nx + (size_t)blockIdx.x * CW;  // row k0, first column
         for (int i = c; i < 8 * R; i += CW) {
             const int ai = i / R, m = i - ai * R;
             if (m >= n) continue;
@@ -140,36 +132,6 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         band_publish<CW, R>(bd, bd.uv[2], C0, c, g, k0, n, nz, ra);
     }
     __syncthreads();
-    // L2 prefetch of the next tile's first-phase inputs (xi_z, v_z, RHS v_z of stage s-2 of
-    // this thread group's rows) and of its PML rows, one 128-byte line per (array, row)
-    if (CW == 32 && tile + (int)gridDim.x < ntiles) {
-        const int nt = tile + gridDim.x, nbx = nt % tiles_x, nb_ = nt / tiles_x;
-        const float *An = a.A + (size_t)nb_ * 4 * F;
-        const size_t ob = (size_t)k0 * nx + (size_t)nbx * CW;
-        for (int i = c; i < 3 * R; i += CW) {
-            const int ai = i / R, m = i - ai * R;
-            if (m >= n) continue;
-            const float *p = ai == 0 ? An + F_XIZ * F : ai == 1 ? An + F_VZ * F
-                                                                 : (s >= 3 ? svp(a, a.slot_sm2, nb_, 1) : nullptr);
-            if (p) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + ob + (size_t)m * nx) : "memory");
-        }
-        for (int i = threadIdx.x; i < 7 * nzp; i += blockDim.x) {
-            const int ai = i / nzp, pi = i - ai * nzp;
-            const size_t qz = ((size_t)nb_ * 2 * nzp + pi) * nx + (size_t)nbx * CW;
-            const size_t qb = (size_t)nb_ * a.bgz + (size_t)pi * nx + (size_t)nbx * CW;
-            const float *p;
-            switch (ai) {
-                case 0: p = a.PZ + qz; break;
-                case 1: p = a.PZ + qz + (size_t)nzp * nx; break;
-                case 2: p = a.SPZ + a.slot_sm1 * spz_slot + qz; break;
-                case 3: p = a.SPZ + a.slot_sm1 * spz_slot + qz + (size_t)nzp * nx; break;
-                case 4: p = a.az + qb; break;
-                case 5: p = a.bz + qb; break;
-                default: p = a.fdz + qb; break;
-            }
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(p) : "memory");
-        }
-    }
     // ---- 3: d xi_z/dz, vertical PML, divergence, pressure (kept in FA); v_x of stage s
     {
         float d[R];
@@ -218,7 +180,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         if (m < n) a.P[(size_t)b * F + (size_t)(k0 + m) * nx + x] = FA[(k0 + m) * CW + c];
     for (int i = threadIdx.x; i < nzp * CW; i += blockDim.x) {  // new RHS of psi_vz (phase 3)
         const int pi = i / CW, cc = i - pi * CW;
-        a.SPZ[a.slot_s * spz_slot + ((size_t)b * 2 * nzp + pi) * nx + bx * CW + cc] = PS[(0 * nzp + pi) * CW + cc];
+        a.SPZ[a.slot_s * spz_slot + ((size_t)b * 2 * nzp + pi) * nx + blockIdx.x * CW + cc] = PS[(0 * nzp + pi) * CW + cc];
     }
     __syncthreads();
     // ---- 5: gradient of p, RHS v_z without advection; advection of v_x along z (partial RHS
@@ -310,10 +272,8 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     }
     for (int i = threadIdx.x; i < nzp * CW; i += blockDim.x) {  // new RHS of psi_p (phase 5)
         const int pi = i / CW, cc = i - pi * CW;
-        a.SPZ[a.slot_s * spz_slot + ((size_t)b * 2 * nzp + pi + nzp) * nx + bx * CW + cc] =
+        a.SPZ[a.slot_s * spz_slot + ((size_t)b * 2 * nzp + pi + nzp) * nx + blockIdx.x * CW + cc] =
             PS[(1 * nzp + pi) * CW + cc];
-    }
-    __syncthreads();  // the next tile overwrites the shared tiles and PML rows
     }
 }
 
@@ -361,17 +321,11 @@ static cudaError_t launch_band(const StepArgs<float> &a, const BandDev &bd, cuda
     if (G > band_maxg<CW>() || a.nx % CW != 0 || R * G - a.nz >= R) return cudaErrorInvalidValue;
     if ((NX && a.nx != NX) || (NZ && a.nz != NZ)) return cudaErrorInvalidValue;
     const size_t smem = band_smem<CW, R>(a.nz, a.nzpml);
-    auto kern = col_band_kernel<CW, R, NX, NZ>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(col_band_kernel<CW, R, NX, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
-    // persistent grid: as many blocks as fit on the device at once, each looping over tiles
-    int dev = 0, nsm = 0, per_sm = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, G * CW, smem)) != cudaSuccess) return e;
-    const int ntiles = (a.nx / CW) * a.nb;
-    const int nblk = std::max(1, std::min(ntiles, nsm * std::max(per_sm, 1)));
-    kern<<<nblk, G * CW, smem, st>>>(a, bd);
+    dim3 grid(a.nx / CW, a.nb);
+    col_band_kernel<CW, R, NX, NZ><<<grid, G * CW, smem, st>>>(a, bd);
     return cudaGetLastError();
 }
 
