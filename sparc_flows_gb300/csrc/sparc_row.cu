@@ -9,7 +9,6 @@
 //                                 the column pass needs for its ibc=3 boundary);
 //   d/dx of v_x, v_z at stage s -> advection terms -2 v0x d/dx (physics2d.f90:1065-1079).
 #include "sparc_fft512.cuh"
-#include "sparc_tma.cuh"
 
 namespace sparc {
 
@@ -183,8 +182,7 @@ __global__ void __launch_bounds__(ROW_WPB *WARP) row_stage_kernel(StepArgs<T> a)
 // psi_gradp_x RHS; closing pass, the new psi_gradp_x).  The stores follow in row_mid_store.
 template <int MODE>
 __device__ __forceinline__ void row_mid_load(const StepArgs<float> &a, const RowCtx<float> &r, int x, float gpx,
-                                             float dxx, float *P, const float *RW, float &svx, float &dxo, float &vxs,
-                                             float &vzs)
+                                             float dxx, float *P, float &svx, float &dxo, float &vxs, float &vzs)
 {
     const int b = r.b, k = r.k, nx = r.nx, nh = r.nh, nhx = r.nhx;
     const size_t F = r.F, ro = r.ro;
@@ -213,27 +211,22 @@ __device__ __forceinline__ void row_mid_load(const StepArgs<float> &a, const Row
             P[2 * nhx + ai] = r.PXb[q1] + a.dt * ngp;
         }
     }
-    // RW: this row's bulk-copied inputs (row_bulk_rows): MODE 1 RVXP, v_x, v_z, RHS v_z of stage
-    // s-1; MODE 0 v_x, v_z; MODE 2 RVXP
     svx = 0.f;
     if (MODE != 0) {
-        svx = RW[x] - r.rhoinv_k * gpx;
+        svx = __ldg(a.RVXP + (size_t)b * F + ro + x) - r.rhoinv_k * gpx;
         if (k == 0 || x == 0 || x == nx - 1) svx = 0.f;
     }
     dxo = dxx;
     vxs = 0.f;
     vzs = 0.f;
     if (MODE != 2) {
-        const int o = MODE == 1 ? 512 : 0;
-        vxs = RW[o + x];
-        vzs = RW[o + 512 + x];
+        vxs = __ldg(r.Ab + F_VX * F + ro + x);
+        vzs = __ldg(r.Ab + F_VZ * F + ro + x);
         if (MODE == 1) {
             vxs += r.bs * svx;
-            vzs += r.bs * RW[3 * 512 + x];
+            vzs += r.bs * __ldg(svp(a, a.slot_sm1, b, 1) + ro + x);
         }
     }
-    (void)F;
-    (void)ro;
 }
 
 // The x-PML stores of row_mid_load from the warp scratch P (lanes over the PML columns).
@@ -254,13 +247,6 @@ __device__ __forceinline__ void row_mid_store_pml(const StepArgs<float> &a, cons
     }
 }
 
-// Rows of the second part of the register-FFT pass, copied to shared memory by one bulk copy each
-// at kernel start so that they arrive while the first transform runs.
-template <int MODE>
-constexpr int row_bulk_rows() { return MODE == 1 ? 4 : (MODE == 0 ? 2 : 1); }
-constexpr int ROW512_WARP_FLOATS = FFT512_SCRATCH + 4 * 512 + 4;  // scratch, bulk rows, mbarrier
-constexpr uint32_t ROW_WAIT_ITERS = 1u << 24;
-
 // FP32 rows of 512 columns: the same row pass with the register-resident FFT (sparc_fft512.cuh);
 // register n2 of a lane holds column lane + 32 n2.  Each part loads everything it needs before it
 // stores anything, so no load waits behind a store of the row it may alias.
@@ -272,31 +258,8 @@ __global__ void __launch_bounds__(ROW_WPB *WARP, 4) row_stage_reg512_kernel(Step
     if (MODE == 0 && blockIdx.x == 0 && threadIdx.x == 0) *a.d_time += 1;  // new step begins
     const int row = blockIdx.x * ROW_WPB + warp;
     if (row >= a.nb * a.nz) return;
-    float *S = reinterpret_cast<float *>(smem_raw) + warp * ROW512_WARP_FLOATS;
-    float *RW = S + FFT512_SCRATCH;  // bulk-copied rows [row_bulk_rows][512]
-    uint64_t *bar = reinterpret_cast<uint64_t *>(RW + 4 * 512);
+    float *S = reinterpret_cast<float *>(smem_raw) + warp * FFT512_SCRATCH;
     const RowCtx<float> r(a, row, 512);
-    constexpr int NBULK = row_bulk_rows<MODE>();
-    if (lane == 0) {
-        const float *src[4];
-        if (MODE == 1) {
-            src[0] = a.RVXP + (size_t)r.b * r.F + r.ro;
-            src[1] = r.Ab + F_VX * r.F + r.ro;
-            src[2] = r.Ab + F_VZ * r.F + r.ro;
-            src[3] = svp(a, a.slot_sm1, r.b, 1) + r.ro;
-        } else if (MODE == 0) {
-            src[0] = r.Ab + F_VX * r.F + r.ro;
-            src[1] = r.Ab + F_VZ * r.F + r.ro;
-        } else {
-            src[0] = a.RVXP + (size_t)r.b * r.F + r.ro;
-        }
-        mbar_init(bar, 1);
-        fence_mbar_init();
-        mbar_arrive_expect_tx(bar, NBULK * 512 * sizeof(float));
-#pragma unroll
-        for (int i = 0; i < NBULK; i++) bulk_load_1d(RW + i * 512, src[i], 512 * sizeof(float), bar);
-    }
-    __syncwarp();
 
     float re[16], im[16];
     float mr = 0.f, mi = 0.f;
@@ -314,15 +277,10 @@ __global__ void __launch_bounds__(ROW_WPB *WARP, 4) row_stage_reg512_kernel(Step
     float mr2 = 0.f, mi2 = 0.f;
     float svx[16], dxo[16];
     __syncwarp();  // the transform's last reads of S are done before S holds the x-PML values
-    if (!mbar_wait_bounded(bar, 0, ROW_WAIT_ITERS)) {  // the bulk rows did not arrive: flag it
-        if (lane == 0) atomicExch(a.d_err, SPARC_DEV_ERR_TMA_TIMEOUT);
-        mbar_wait_bounded(bar, 0, ROW_WAIT_ITERS);  // the copies may still land: wait (bounded)
-        return;
-    }
 #pragma unroll
     for (int n2 = 0; n2 < 16; n2++) {
         float vxs, vzs;
-        row_mid_load<MODE>(a, r, lane + 32 * n2, re[n2] * isr, im[n2] * isi, S, RW, svx[n2], dxo[n2], vxs, vzs);
+        row_mid_load<MODE>(a, r, lane + 32 * n2, re[n2] * isr, im[n2] * isi, S, svx[n2], dxo[n2], vxs, vzs);
         re[n2] = vxs;
         im[n2] = vzs;
         mr2 = fmaxf(mr2, fabsf(vxs));
@@ -405,8 +363,7 @@ bool fft_size_supported(int n)
 template <int MODE>
 static void row_reg512_launch(const StepArgs<float> &a, int grid, cudaStream_t st)
 {
-    const size_t smem = (size_t)ROW_WPB * ROW512_WARP_FLOATS * sizeof(float);
-    cudaFuncSetAttribute(row_stage_reg512_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = (size_t)ROW_WPB * FFT512_SCRATCH * sizeof(float);
     row_stage_reg512_kernel<MODE><<<grid, ROW_WPB * WARP, smem, st>>>(a);
 }
 

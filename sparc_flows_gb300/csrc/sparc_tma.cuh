@@ -66,16 +66,6 @@ __device__ __forceinline__ void tma_load_2d(void *smem_dst, const CUtensorMap *m
         : "memory");
 }
 
-// 1-D bulk copy of `bytes` contiguous bytes global -> shared, completing on `bar` (both addresses
-// 16-byte aligned, bytes a multiple of 16).
-__device__ __forceinline__ void bulk_load_1d(void *smem_dst, const void *src, uint32_t bytes, uint64_t *bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(smem_dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
 // Make this thread's generic-proxy shared-memory accesses visible to / ordered before later
 // async-proxy (TMA) operations on the same shared memory.
 __device__ __forceinline__ void fence_proxy_async_smem()
