@@ -12,9 +12,11 @@ backward = the reference's adjoint: the incoming gradient at the receivers, time
 
 For L = 1/2 |seis - data|^2 the incoming gradient is the waveform residual, so backward runs
 exactly the reference's adjoint + kernel stage.  The reference's adjoint is a continuous
-(time-reversal) adjoint: kernel_psi equals dL/dpsi up to the reference's fixed normalisation
-(its dimensional units) and the discretisation error of the continuous adjoint, which is what
-its line searches rely on.  ``fd_check`` measures both against central finite differences.
+(time-reversal) adjoint and kernel_psi a density: kernel_psi times the cell height dz equals
+dL/dpsi up to the reference's fixed normalisation (its units and sign) below the receiver layer,
+but not in the top rows that hold the receiver / adjoint-source row and the top PML, where the
+time-reversed solve is not the discrete adjoint (measured in tests/test_gpu_reference_kernel.py).
+``fd_check`` measures it against central finite differences, with the dz pairing if given.
 
 The exact gradient of the same seismograms is ``exact_records`` (discrete_adjoint.py): its
 backward is the transpose of the device step itself, replayed from HBM checkpoints, and agrees
@@ -55,10 +57,11 @@ def seismograms(psi: torch.Tensor, pipe: FwdAdjKernels) -> torch.Tensor:
 
 
 def fd_check(pipe: FwdAdjKernels, psi: torch.Tensor, data: torch.Tensor, directions: list[torch.Tensor],
-             eps: float) -> dict:
+             eps: float, weight: torch.Tensor | None = None) -> dict:
     """Central finite differences of L(psi) = 1/2 |seis(psi) - data|^2 along each direction
-    against <grad, direction> from backward.  Returns the per-direction ratios FD / <grad, d>:
-    their spread measures the gradient's direction error, their mean the normalisation."""
+    against <grad, direction> from backward (weighted by ``weight``, e.g. the cell height dz per
+    row, if given).  Returns the per-direction ratios FD / <grad, d>: their spread measures the
+    gradient's direction error, their mean the normalisation."""
     psi = psi.detach().clone().requires_grad_(True)
     loss = 0.5 * ((seismograms(psi, pipe) - data) ** 2).sum()
     loss.backward()
@@ -69,7 +72,7 @@ def fd_check(pipe: FwdAdjKernels, psi: torch.Tensor, data: torch.Tensor, directi
             lp = 0.5 * ((seismograms(psi.detach() + eps * d, pipe) - data) ** 2).sum().item()
             lm = 0.5 * ((seismograms(psi.detach() - eps * d, pipe) - data) ** 2).sum().item()
         fd = (lp - lm) / (2.0 * eps)
-        dot = float((g * d).sum().item())
+        dot = float((g * d * (weight if weight is not None else 1.0)).sum().item())
         fds.append(fd)
         dots.append(dot)
         ratios.append(fd / dot if dot != 0.0 else float("nan"))
