@@ -81,29 +81,6 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         PS[(4 * nzp + pi) * CW + cc] = __ldg(a.fdz + qb);
     }
 
-    // L2 prefetch of the later phases' per-point inputs of this thread group's rows: one
-    // 128-byte line per (array, row) for CW = 32, spread over the lanes, no registers held, so
-    // those loads find their lines in L2 instead of waiting on DRAM phase by phase
-    if constexpr (CW == 32) {
-        const size_t ob = (size_t)k0 * nx + (size_t)blockIdx.x * CW;  // row k0, first column
-        for (int i = c; i < 8 * R; i += CW) {
-            const int ai = i / R, m = i - ai * R;
-            if (m >= n) continue;
-            const float *p;
-            switch (ai) {
-                case 0: p = a.DX + (size_t)b * F; break;
-                case 1: p = Ab + F_VX * F; break;
-                case 2: p = s >= 2 ? svp(a, a.slot_sm1, b, 0) : nullptr; break;
-                case 3: p = a.flows ? a.FXX + (size_t)b * F : nullptr; break;
-                case 4: p = s >= 2 ? svp(a, a.slot_sm1, b, 1) : nullptr; break;
-                case 5: p = a.flows ? a.FXZ + (size_t)b * F : nullptr; break;
-                case 6: p = a.c2d ? a.c2rho0 + (size_t)b * a.bg2 : nullptr; break;
-                default: p = a.flows ? a.v0z + (size_t)b * a.bg2 : nullptr; break;
-            }
-            if (p) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + ob + (size_t)m * nx) : "memory");
-        }
-    }
-
     // ---- 1: xi_z at stage s (scr xi_z = v_z of stage s-1 with the RHS boundary zeros)
     float xz[R];
 #pragma unroll
@@ -124,6 +101,25 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         }
     }
     __syncthreads();
+    // L2 prefetch of phase 3's per-point inputs of this thread group's rows (one 128-byte line
+    // per array and row, spread over the lanes, no registers held), issued once phase 1's own
+    // loads have been served so that they do not compete with them
+    if constexpr (CW == 32) {
+        const size_t ob = (size_t)k0 * nx + (size_t)blockIdx.x * CW;
+        for (int i = c; i < 4 * R; i += CW) {
+            const int ai = i / R, m = i - ai * R;
+            if (m >= n) continue;
+            const float *p;
+            switch (ai) {
+                case 0: p = a.DX + (size_t)b * F; break;
+                case 1: p = Ab + F_VX * F; break;
+                case 2: p = s >= 2 ? svp(a, a.slot_sm1, b, 0) : nullptr; break;
+                case 3: p = a.c2d ? a.c2rho0 + (size_t)b * a.bg2 : nullptr; break;
+                default: p = nullptr; break;
+            }
+            if (p) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + ob + (size_t)m * nx) : "memory");
+        }
+    }
     // ---- 2: right-hand side of d xi_z/dz (ibc 3, top value -dxi_x/dx * unstretch)
     {
         float ra[R];
@@ -132,6 +128,23 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
         band_publish<CW, R>(bd, bd.uv[2], C0, c, g, k0, n, nz, ra);
     }
     __syncthreads();
+    // ... and of phases 5 and 7's inputs, issued as phase 3 starts
+    if constexpr (CW == 32) {
+        const size_t ob = (size_t)k0 * nx + (size_t)blockIdx.x * CW;
+        for (int i = c; i < 4 * R; i += CW) {
+            const int ai = i / R, m = i - ai * R;
+            if (m >= n) continue;
+            const float *p;
+            switch (ai) {
+                case 0: p = a.flows ? a.FXX + (size_t)b * F : nullptr; break;
+                case 1: p = s >= 2 ? svp(a, a.slot_sm1, b, 1) : nullptr; break;
+                case 2: p = a.flows ? a.FXZ + (size_t)b * F : nullptr; break;
+                case 3: p = a.flows ? a.v0z + (size_t)b * a.bg2 : nullptr; break;
+                default: p = nullptr; break;
+            }
+            if (p) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + ob + (size_t)m * nx) : "memory");
+        }
+    }
     // ---- 3: d xi_z/dz, vertical PML, divergence, pressure (kept in FA); v_x of stage s
     {
         float d[R];
