@@ -606,6 +606,27 @@ def run_3d(args):
         torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e = units / args.steps * max(1, args.steps) / e2e_s
+    ws.close()
+    # forward + adjoint + kernel integral of the same batch with the forward field checkpointed in
+    # HBM every 100 steps and recomputed per segment (pipeline3d); a run of `fa_steps` steps
+    from sparc_flows_gb300.pipeline3d import FwdAdjKernels3D
+    fa_steps = args.nsteps or 200
+    fak = FwdAdjKernels3D(nx, ny, model, xl, pats, amp, fa_steps, flow=v0, precision=32, steps_out=15,
+                          checkpoint_every=100, device=f"cuda:{local}")
+    fak.run_all()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    fak.run_all()
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fa_ms = f0.elapsed_time(f1)
+    fwd_adj = {"workload": f"{nsrc} sources, {nx} x {ny} x {nz}, {fa_steps} steps, forward + adjoint + kernel "
+                           "integral, checkpoint every 100 steps (recomputed per segment)",
+               "value": fak.point_steps() / (fa_ms * 1e-3), "unit": UNIT, "ms_per_run": fa_ms,
+               "solves_per_run": 3, "records": fak.nrec, "checkpoint_bytes": int(fak.ckpt.numel()),
+               "record_buffer_bytes": int(fak.snaps.numel() * fak.snaps.element_size())}
+    fak.close()
     words = 15 * 6 + 10 + 5 * 3 + 15 * (2 * 20 / nz)  # 15 V + 10 + 5 B + 15 Naux/N, 20 PML levels: 117 words
     peak, peak_kind = measured_peak_hbm()
     achieved = words * 4 * value / 1e9
@@ -620,9 +641,8 @@ def run_3d(args):
             "clocks": clk.summary(),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": amp_h.numel() * 8,
                     "d2h_bytes_per_step": int(rec_h.numel() * 4)},
-            "gpu_launches": None}
+            "gpu_launches": None, "fwd_adj_kernels": fwd_adj}
     print(json.dumps(line), flush=True)
-    ws.close()
 
 
 def main():

@@ -293,6 +293,38 @@ int sparc3d_forward(sparc3d_plan_t *plan, int nsteps, void *seis, int nrec_cap, 
 int sparc3d_get_state(sparc3d_plan_t *plan, void *dst, void *stream);
 int sparc3d_set_state(sparc3d_plan_t *plan, const void *src, void *stream);
 
+/* Kernel-mode adjoint source (displacement.f90:615-627, LAGRANGE_INTERP physics.f90:678-737): at
+ * step t the forcing added to RHS v_z at level k_obs is
+ *   scale * sum_j wts[t][j] * rows[b][idx[t] + j][y][x],  j = 0..6
+ * (rows beyond nrows count as zero; no forcing for t >= ntab), scale = delta_width / rho0(o_rad);
+ * it replaces the pattern source.  rows: DEVICE FP64 [nbatch][nrows][ny][nx], kept by pointer
+ * (it must stay valid while the plan steps); wts [ntab][7], idx [ntab]: host, copied. */
+int sparc3d_set_adjoint_source(sparc3d_plan_t *plan, const double *rows, int nrows, const double *wts, const int *idx,
+                               int ntab, double scale, void *stream);
+
+/* sparc3d_forward that also writes kernel-stage records: after a step whose index t is a
+ * multiple of steps_out, record j = t / steps_out, if rec0 <= j < rec0 + snap_cap, goes to slot
+ * j - rec0 of snaps (DEVICE, plan precision, [snap_cap][5][nz][nbatch][ny][nx]): div xi (x, y
+ * and filtered z derivatives, FILTER_VAR_Z kernels.f90:891-928), v_x, v_y, v_z and |acc|^2 of the
+ * last stage's RHS of v -- what the kernel integral reads of the forward partial states
+ * (kernels.f90:221-280) in a 3-D restatement of the 2-D kernel stage. */
+int sparc3d_forward_records(sparc3d_plan_t *plan, int nsteps, void *seis, int nrec_cap, int *nrec, void *snaps,
+                            int rec0, int snap_cap, void *stream);
+
+/* One record pair of the 3-D kernel integral (kernels.f90:293-358 with a y term; the reference's
+ * kernel stage is 2-D only, kernels.f90:32): with the plan's CURRENT state as the adjoint fields
+ * and slot `slot` of snaps (as written by sparc3d_forward_records) as the forward record, add in
+ * FP64 to out ([5][nz][nbatch][ny][nx], DEVICE): div xi_f div v_a, sum_j d_x(v_f,j) v_a,j,
+ * sum_j d_y(v_f,j) v_a,j, sum_j d_z(v_f,j) v_a,j (z derivatives filtered) and |acc_f|^2. */
+int sparc3d_kernels_accumulate(sparc3d_plan_t *plan, const void *snaps, int slot, double *out, void *stream);
+
+/* Checkpoint of what a step carries to the next (state and PML auxiliaries): the reference has
+ * none (it restarts from its full dumps).  save copies sparc3d_checkpoint_bytes(plan) bytes to a
+ * 16-byte aligned DEVICE buffer and returns the step counter in *time; load restores both. */
+size_t sparc3d_checkpoint_bytes(const sparc3d_plan_t *plan);
+int sparc3d_checkpoint_save(sparc3d_plan_t *plan, void *dst, int *time, void *stream);
+int sparc3d_checkpoint_load(sparc3d_plan_t *plan, const void *src, int time, void *stream);
+
 /* ---------------------------------------------------------------------------------------------
  * 2-D velocity-pressure-density solver: option 5, MP_QUIET_SPONGE_2D (physics2d.f90:1099-1137,
  * a sponge layer, USE_PML off), option 6, MP_QUIET_PML_2D (physics2d.f90:662-713, the

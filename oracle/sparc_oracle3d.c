@@ -68,6 +68,11 @@ typedef struct {
     double *fre, *fim, *ftr, *fti;
     double *pattern, *amp;
     int namp;
+    /* kernel-mode adjoint source (displacement.f90:615-627): slices [nrows][ny][nx] and the
+     * per-step LAGRANGE_INTERP table (physics.f90:678-737) */
+    int adj, adj_nrows, adj_ntab;
+    double *adj_rows, *adj_w, adj_scale;
+    int *adj_idx;
     int time;
 } orc3_sim;
 
@@ -250,8 +255,10 @@ void orc3_destroy(orc3_sim *s)
     double *ptrs[] = {s->fre, s->fim, s->ftr, s->fti, s->z, s->stretch, s->unstretch, s->g, s->source_dep,
                       s->rho0, s->p0, s->c2, s->rhoinv, s->c2rho0, s->gradrho0_z, s->gradp0_z, s->az, s->bzpml,
                       s->v0x, s->v0y, s->v0z, s->a, s->temp, s->scr, s->pmlvars, s->psipml, s->scrpml,
-                      s->d1, s->d2, s->d3, s->div, s->pp, s->rho, s->gpx, s->gpy, s->gpz, s->pattern, s->amp};
+                      s->d1, s->d2, s->d3, s->div, s->pp, s->rho, s->gpx, s->gpy, s->gpz, s->pattern, s->amp,
+                      s->adj_rows, s->adj_w};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); i++) free(ptrs[i]);
+    free(s->adj_idx);
     orc_fft_delete(s->fx);
     orc_fft_delete(s->fy);
     free(s);
@@ -273,6 +280,28 @@ int orc3_set_source(orc3_sim *s, const double *pattern, const double *amp, int n
     s->amp = z3(namp);
     memcpy(s->amp, amp, (size_t)namp * sizeof(double));
     s->namp = namp;
+    return 0;
+}
+
+/* Kernel-mode adjoint source: forcing(x, y, step t) = scale * sum_j w[t][j] rows[idx[t] + j](x, y),
+ * injected into RHS v_z at o_rad in place of the pattern source. */
+int orc3_set_adjoint_source(orc3_sim *s, const double *rows, int nrows, const double *w, const int *idx, int ntab,
+                            double scale)
+{
+    const size_t nxy = (size_t)s->nx * s->ny;
+    free(s->adj_rows);
+    free(s->adj_w);
+    free(s->adj_idx);
+    s->adj_rows = z3((size_t)nrows * nxy);
+    memcpy(s->adj_rows, rows, (size_t)nrows * nxy * sizeof(double));
+    s->adj_w = z3((size_t)ntab * 7);
+    memcpy(s->adj_w, w, (size_t)ntab * 7 * sizeof(double));
+    s->adj_idx = (int *)calloc((size_t)ntab, sizeof(int));
+    memcpy(s->adj_idx, idx, (size_t)ntab * sizeof(int));
+    s->adj_nrows = nrows;
+    s->adj_ntab = ntab;
+    s->adj_scale = scale;
+    s->adj = 1;
     return 0;
 }
 
@@ -341,7 +370,19 @@ static void orc3_rhs(orc3_sim *s)
         for (size_t q = 0; q < nxy; q++) {
             const size_t i = (size_t)k * nxy + q;
             rvz[i] = rvz[i] - s->rhoinv[k] * s->rho[i] * s->g[k];
-            if (abs(k - s->e_rad) <= 4) rvz[i] = rvz[i] + (s->pattern[q] * amp) * s->source_dep[k];
+            if (s->adj) {
+                if (k == s->o_rad && s->time >= 0 && s->time < s->adj_ntab) {
+                    const double *w = s->adj_w + (size_t)s->time * 7;
+                    double f = 0.0;
+                    for (int j = 0; j < 7; j++) {
+                        const int r = s->adj_idx[s->time] + j;
+                        if (r >= 0 && r < s->adj_nrows && w[j] != 0.0) f += w[j] * s->adj_rows[(size_t)r * nxy + q];
+                    }
+                    rvz[i] = rvz[i] + f * s->adj_scale;
+                }
+            } else if (abs(k - s->e_rad) <= 4) {
+                rvz[i] = rvz[i] + (s->pattern[q] * amp) * s->source_dep[k];
+            }
         }
     memcpy(s->scr, vx, N * sizeof(double));
     memcpy(s->scr + N, vy, N * sizeof(double));
@@ -409,6 +450,20 @@ int orc3_run(orc3_sim *s, int nsteps, double *seis)
         s->time++;
     }
     return nrec;
+}
+
+/* One step of TIMESTEPPING; returns the index of the step made (the record test of orc3_run). */
+int orc3_advance(orc3_sim *s)
+{
+    orc3_step(s);
+    return s->time++;
+}
+
+/* RHS of the last stage of the last step, [6][nz][ny][nx] (the acceleration is entries 3..5). */
+int orc3_get_scr(const orc3_sim *s, double *scr)
+{
+    memcpy(scr, s->scr, 6 * s->N * sizeof(double));
+    return 0;
 }
 
 /* the whole state [6][nz][ny][nx] and the PML auxiliaries [2][nzpml][ny][nx] */

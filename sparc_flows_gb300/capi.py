@@ -58,6 +58,14 @@ SIGNATURES = {
     "sparc3d_forward": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, _ip, _vp]),
     "sparc3d_get_state": (ctypes.c_int, [_vp, _vp, _vp]),
     "sparc3d_set_state": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sparc3d_set_adjoint_source": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _dp, _ip, ctypes.c_int, ctypes.c_double,
+                                                  _vp]),
+    "sparc3d_forward_records": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int, _ip, _vp, ctypes.c_int,
+                                               ctypes.c_int, _vp]),
+    "sparc3d_kernels_accumulate": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _vp]),
+    "sparc3d_checkpoint_bytes": (ctypes.c_size_t, [_vp]),
+    "sparc3d_checkpoint_save": (ctypes.c_int, [_vp, _vp, _ip, _vp]),
+    "sparc3d_checkpoint_load": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp]),
     "sparc5_plan_create": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "sparc5_plan_destroy": (ctypes.c_int, [_vp]),
     "sparc5_set_background": (ctypes.c_int, [_vp, _vp, _vp]),

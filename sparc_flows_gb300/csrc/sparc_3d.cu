@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(S3_THREADS) s3_rhs_kernel(S3Args a, S3Bg<T> bg
                                                             const T *__restrict__ GY, const T *__restrict__ GZ,
                                                             const T *__restrict__ PSIP, T *__restrict__ SPSIP,
                                                             const T *__restrict__ RHO, const T *__restrict__ PAT,
-                                                            T amp)
+                                                            T amp, const T *__restrict__ ADJ, int k_obs)
 {
     const long long lvl = (long long)a.nb * a.nxy, n = lvl * a.nz, F = n;
     const long long stride = (long long)gridDim.x * S3_THREADS;
@@ -213,7 +213,11 @@ __global__ void __launch_bounds__(S3_THREADS) s3_rhs_kernel(S3Args a, S3Bg<T> bg
         const T az = a.flows ? SCR[5 * F + i] : T(0);
         T rz = az - ri * gz;
         rz = rz - ri * RHO[i] * bg.g[k];
-        if (abs(k - a.e_rad) <= 4) rz = rz + (PAT[r] * amp) * bg.source_dep[k];
+        if (ADJ) {  // kernel-mode adjoint: forcing / rho0 * delta_width at o_rad (displacement.f90:615-627)
+            if (k == k_obs) rz = rz + ADJ[r];
+        } else if (abs(k - a.e_rad) <= 4) {
+            rz = rz + (PAT[r] * amp) * bg.source_dep[k];
+        }
         SCR[3 * F + i] = ax - ri * GX[i];
         SCR[4 * F + i] = ay - ri * GY[i];
         SCR[5 * F + i] = rz;
@@ -255,6 +259,77 @@ __global__ void __launch_bounds__(S3_THREADS) s3_end_kernel(S3Args a, T *__restr
         for (int j = 0; j < 10; j++) w[j] = w[j + 1];
         if (k + 6 < a.nz) w[10] = col[(long long)(k + 6) * lvl];
         col[(long long)k * lvl] = out;
+    }
+}
+
+// Adjoint forcing of one step at the observation level, [nb][ny][nx]: LAGRANGE_INTERP of the
+// adjoint-source slices (physics.f90:678-737), forcing = sum_j w[j] rows[b][i0 + j] (rows outside
+// 0 .. nrows-1 count as zero), times scale = delta_width / rho0(o_rad).
+template <typename T>
+__global__ void __launch_bounds__(S3_THREADS) s3_adjsrc_kernel(long long lvl, long long nxy, const double *__restrict__ rows,
+                                                               int nrows, int i0, S3Lagr w, double scale,
+                                                               T *__restrict__ ADJ)
+{
+    const long long stride = (long long)gridDim.x * S3_THREADS;
+    for (long long i = (long long)blockIdx.x * S3_THREADS + threadIdx.x; i < lvl; i += stride) {
+        const long long b = i / nxy, q = i - b * nxy;
+        double f = 0.0;
+#pragma unroll
+        for (int j = 0; j < 7; j++) {
+            const int r = i0 + j;
+            if (r >= 0 && r < nrows && w.w[j] != 0.0) f += w.w[j] * rows[((size_t)b * nrows + r) * nxy + q];
+        }
+        ADJ[i] = (T)(f * scale);
+    }
+}
+
+// Kernel-stage record of the forward state (what PRODUCE_KERNELS reads from the partial states,
+// kernels.f90:221-280): div xi = D1 + D2 + D3 (the x, y and filtered z derivatives), v_x, v_y, v_z,
+// and |acc|^2 of the last stage's RHS of v (hessian integrand), [5][F].
+template <typename T>
+__global__ void __launch_bounds__(S3_THREADS) s3_record_kernel(long long F, const T *__restrict__ D1,
+                                                               const T *__restrict__ D2, const T *__restrict__ D3,
+                                                               const T *__restrict__ A, const T *__restrict__ SCR,
+                                                               T *__restrict__ snap)
+{
+    const long long stride = (long long)gridDim.x * S3_THREADS;
+    for (long long i = (long long)blockIdx.x * S3_THREADS + threadIdx.x; i < F; i += stride) {
+        snap[i] = D1[i] + D2[i] + D3[i];
+        snap[F + i] = A[3 * F + i];
+        snap[2 * F + i] = A[4 * F + i];
+        snap[3 * F + i] = A[5 * F + i];
+        const double ax = SCR[3 * F + i], ay = SCR[4 * F + i], az = SCR[5 * F + i];
+        snap[4 * F + i] = (T)(ax * ax + ay * ay + az * az);
+    }
+}
+
+// Kernel integrands, FP64 accumulation into out [5][F] (kc, kv_x, kv_y, kv_z, hessian):
+// kc += div xi_f div v_a (div v_a = D1 + D2 + D3 of the adjoint v), hessian += |acc_f|^2.
+template <typename T>
+__global__ void __launch_bounds__(S3_THREADS) s3_kacc_div_kernel(long long F, const T *__restrict__ D1,
+                                                                 const T *__restrict__ D2, const T *__restrict__ D3,
+                                                                 const T *__restrict__ snap, double *__restrict__ out)
+{
+    const long long stride = (long long)gridDim.x * S3_THREADS;
+    for (long long i = (long long)blockIdx.x * S3_THREADS + threadIdx.x; i < F; i += stride) {
+        const T diva = D1[i] + D2[i] + D3[i];
+        out[i] += (double)snap[i] * (double)diva;
+        out[4 * F + i] += (double)snap[4 * F + i];
+    }
+}
+
+// kv_i += d_i(v_f,j) v_a,j for one component j (D1, D2, D3: x, y, filtered z derivatives of v_f,j).
+template <typename T>
+__global__ void __launch_bounds__(S3_THREADS) s3_kacc_v_kernel(long long F, const T *__restrict__ D1,
+                                                               const T *__restrict__ D2, const T *__restrict__ D3,
+                                                               const T *__restrict__ va, double *__restrict__ out)
+{
+    const long long stride = (long long)gridDim.x * S3_THREADS;
+    for (long long i = (long long)blockIdx.x * S3_THREADS + threadIdx.x; i < F; i += stride) {
+        const double a = va[i];
+        out[F + i] += (double)D1[i] * a;
+        out[2 * F + i] += (double)D2[i] * a;
+        out[3 * F + i] += (double)D3[i] * a;
     }
 }
 
@@ -301,10 +376,44 @@ cudaError_t launch_s3_adv(const S3Args &a, const T *D1, const T *D2, const T *D3
 
 template <typename T>
 cudaError_t launch_s3_rhs(const S3Args &a, const S3Bg<T> &bg, const T *X, T *SCR, const T *GX, const T *GY,
-                          const T *GZ, const T *PSIP, T *SPSIP, const T *RHO, const T *PAT, T amp, cudaStream_t st)
+                          const T *GZ, const T *PSIP, T *SPSIP, const T *RHO, const T *PAT, T amp, const T *ADJ,
+                          int k_obs, cudaStream_t st)
 {
     const long long n = (long long)a.nb * a.nxy * a.nz;
-    s3_rhs_kernel<T><<<s3_grid(n), S3_THREADS, 0, st>>>(a, bg, X, SCR, GX, GY, GZ, PSIP, SPSIP, RHO, PAT, amp);
+    s3_rhs_kernel<T><<<s3_grid(n), S3_THREADS, 0, st>>>(a, bg, X, SCR, GX, GY, GZ, PSIP, SPSIP, RHO, PAT, amp, ADJ,
+                                                        k_obs);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_s3_adjsrc(long long lvl, long long nxy, const double *rows, int nrows, int i0, const S3Lagr &w,
+                             double scale, T *ADJ, cudaStream_t st)
+{
+    s3_adjsrc_kernel<T><<<s3_grid(lvl), S3_THREADS, 0, st>>>(lvl, nxy, rows, nrows, i0, w, scale, ADJ);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_s3_record(long long F, const T *D1, const T *D2, const T *D3, const T *A, const T *SCR, T *snap,
+                             cudaStream_t st)
+{
+    s3_record_kernel<T><<<s3_grid(F), S3_THREADS, 0, st>>>(F, D1, D2, D3, A, SCR, snap);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_s3_kacc_div(long long F, const T *D1, const T *D2, const T *D3, const T *snap, double *out,
+                               cudaStream_t st)
+{
+    s3_kacc_div_kernel<T><<<s3_grid(F), S3_THREADS, 0, st>>>(F, D1, D2, D3, snap, out);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_s3_kacc_v(long long F, const T *D1, const T *D2, const T *D3, const T *va, double *out,
+                             cudaStream_t st)
+{
+    s3_kacc_v_kernel<T><<<s3_grid(F), S3_THREADS, 0, st>>>(F, D1, D2, D3, va, out);
     return cudaGetLastError();
 }
 
@@ -329,7 +438,16 @@ cudaError_t launch_s3_end(const S3Args &a, T *A, const T *SCR, T dt, int filter,
     template cudaError_t launch_s3_adv<T>(const S3Args &, const T *, const T *, const T *, const T *, const T *,     \
                                           const T *, T *, cudaStream_t);                                             \
     template cudaError_t launch_s3_rhs<T>(const S3Args &, const S3Bg<T> &, const T *, T *, const T *, const T *,     \
-                                          const T *, const T *, T *, const T *, const T *, T, cudaStream_t);         \
+                                          const T *, const T *, T *, const T *, const T *, T, const T *, int,        \
+                                          cudaStream_t);                                                             \
+    template cudaError_t launch_s3_adjsrc<T>(long long, long long, const double *, int, int, const S3Lagr &, double, \
+                                             T *, cudaStream_t);                                                     \
+    template cudaError_t launch_s3_record<T>(long long, const T *, const T *, const T *, const T *, const T *, T *,  \
+                                             cudaStream_t);                                                          \
+    template cudaError_t launch_s3_kacc_div<T>(long long, const T *, const T *, const T *, const T *, double *,      \
+                                               cudaStream_t);                                                        \
+    template cudaError_t launch_s3_kacc_v<T>(long long, const T *, const T *, const T *, const T *, double *,        \
+                                             cudaStream_t);                                                          \
     template cudaError_t launch_s3_end<T>(const S3Args &, T *, const T *, T, int, T *, const T *, cudaStream_t);
 S3_INST(float)
 S3_INST(double)

@@ -1445,6 +1445,7 @@ struct Plan3 {
     T *D1 = nullptr, *D2 = nullptr, *D3 = nullptr, *PP = nullptr, *RHO = nullptr, *GX = nullptr, *GY = nullptr,
       *GZ = nullptr;
     T *prof = nullptr, *v0 = nullptr, *pat = nullptr;
+    T *ADJ = nullptr;  // adjoint forcing of the current step at the observation level [nb][ny][nx]
     DevZ<T> z[2];  // ibc 0, 1
     DevFFT<T> fx, fy;
     S3Bg<T> bg{};
@@ -1460,6 +1461,14 @@ struct sparc3d_plan {
     Plan3<float> s32;
     Plan3<double> s64;
     std::vector<double> amp;
+    // kernel-mode adjoint source (sparc3d_set_adjoint_source): the caller's device slices
+    // [nb][nrows][ny][nx] and the per-step LAGRANGE_INTERP table
+    bool adj = false;
+    const double *adj_rows = nullptr;
+    int adj_nrows = 0;
+    double adj_scale = 0.0;
+    std::vector<double> adj_w;
+    std::vector<int> adj_idx;
     int time = 0;
     bool have_bg = false;
     long long F = 0, P = 0, nxy = 0;
@@ -1487,7 +1496,7 @@ int alloc_plan3(sparc3d_plan *p)
         {&S.D1, (size_t)F}, {&S.D2, (size_t)F}, {&S.D3, (size_t)F}, {&S.PP, (size_t)F}, {&S.RHO, (size_t)F},
         {&S.GX, (size_t)F}, {&S.GY, (size_t)F}, {&S.GZ, (size_t)F},
         {&S.prof, (size_t)(8 * nz + 2 * npml)}, {&S.v0, c.flows ? (size_t)3 * nz * p->nxy : 1},
-        {&S.pat, (size_t)c.nbatch * p->nxy},
+        {&S.pat, (size_t)c.nbatch * p->nxy}, {&S.ADJ, (size_t)c.nbatch * p->nxy},
     };
     for (auto &r : reqs) {
         void *ptr = nullptr;
@@ -1543,11 +1552,11 @@ cudaError_t d3y(sparc3d_plan *p, const T *v, T *dv, cudaStream_t st)
     return launch_ddy<T>(v, dv, c.nz * c.nbatch, c.nx, c.ny, (T)c.stretchy, S.fy.twr, S.fy.twi, S.fy.kap, st);
 }
 template <typename T>
-cudaError_t d3z(sparc3d_plan *p, const T *v, T *dv, int ibc, cudaStream_t st)
+cudaError_t d3z(sparc3d_plan *p, const T *v, T *dv, int ibc, cudaStream_t st, int filter = 0)
 {
     const Plan3<T> &S = plan3<T>(p);
     return launch_ddz<T>(S.z[ibc].tab, p->nch, p->L, v, dv, (int)(p->cfg.nbatch * p->nxy), p->cfg.nz, nullptr,
-                         S.stretch, 0, st);
+                         S.stretch, filter, st);
 }
 
 // MP_FLOWS_PML_3D_DISPL (displacement.f90:377-477) on X (psi: PSI), into SCR and SPV.
@@ -1577,14 +1586,29 @@ cudaError_t rhs3(sparc3d_plan *p, const T *X, const T *PSI, T amp, cudaStream_t 
             R3(launch_s3_adv<T>(a, S.D1, S.D2, S.D3, S.v0, S.v0 + q, S.v0 + 2 * q, S.SCR + (3 + comp) * F, st));
         }
     }
-    R3(launch_s3_rhs<T>(a, S.bg, X, S.SCR, S.GX, S.GY, S.GZ, PSI + P, S.SPV + P, S.RHO, S.pat, amp, st));
+    R3(launch_s3_rhs<T>(a, S.bg, X, S.SCR, S.GX, S.GY, S.GZ, PSI + P, S.SPV + P, S.RHO, S.pat, amp,
+                        p->adj ? S.ADJ : nullptr, c.k_obs, st));
 #undef R3
     return cudaSuccess;
 }
 
 // STEP (step.f90:43-119) and the record of TIMESTEPPING (driver.f90:388-409).
+// Kernel-stage record of the current state into snap ([5][F], see s3_record_kernel).
 template <typename T>
-cudaError_t step3(sparc3d_plan *p, T *seis, int cap, int &nrec, cudaStream_t st)
+cudaError_t record3(sparc3d_plan *p, T *snap, cudaStream_t st)
+{
+    Plan3<T> &S = plan3<T>(p);
+    const long long F = p->F;
+    cudaError_t e;
+    if ((e = d3x<T>(p, S.A, S.D1, st)) != cudaSuccess) return e;
+    if ((e = d3y<T>(p, S.A + F, S.D2, st)) != cudaSuccess) return e;
+    if ((e = d3z<T>(p, S.A + 2 * F, S.D3, 1, st, 1)) != cudaSuccess) return e;
+    return launch_s3_record<T>(F, S.D1, S.D2, S.D3, S.A, S.SCR, snap, st);
+}
+
+template <typename T>
+cudaError_t step3(sparc3d_plan *p, T *seis, int cap, int &nrec, cudaStream_t st, T *snaps = nullptr, int rec0 = 0,
+                  int snap_cap = 0)
 {
     Plan3<T> &S = plan3<T>(p);
     const sparc3d_config_t &c = p->cfg;
@@ -1592,6 +1616,18 @@ cudaError_t step3(sparc3d_plan *p, T *seis, int cap, int &nrec, cudaStream_t st)
     const S3Args a{c.nx, c.ny, c.nz, c.nbatch, c.npmlbot, c.npmltop, c.k_src, c.flows, p->nxy};
     const T amp = (T)(p->time >= 0 && p->time < (int)p->amp.size() ? p->amp[p->time] : 0.0);
     cudaError_t e;
+    if (p->adj) {  // this step's adjoint forcing (the same in all five stages)
+        const long long lvl = (long long)c.nbatch * p->nxy;
+        const int t = p->time;
+        if (t >= 0 && t < (int)p->adj_idx.size()) {
+            S3Lagr w;
+            for (int j = 0; j < 7; j++) w.w[j] = p->adj_w[(size_t)t * 7 + j];
+            e = launch_s3_adjsrc<T>(lvl, p->nxy, p->adj_rows, p->adj_nrows, p->adj_idx[t], w, p->adj_scale, S.ADJ, st);
+        } else {
+            e = cudaMemsetAsync(S.ADJ, 0, lvl * sizeof(T), st);
+        }
+        if (e != cudaSuccess) return e;
+    }
     for (int s = 0; s < 5; s++) {
         const T *X = S.A, *PSI = S.PV;
         if (s > 0) {
@@ -1614,8 +1650,36 @@ cudaError_t step3(sparc3d_plan *p, T *seis, int cap, int &nrec, cudaStream_t st)
             if (e != cudaSuccess) return e;
         }
         nrec++;
+        const int j = p->time / c.steps_out - rec0;  // kernel-stage record j of the window
+        if (snaps && j >= 0 && j < snap_cap) {
+            e = record3<T>(p, snaps + (size_t)j * 5 * F, st);
+            if (e != cudaSuccess) return e;
+        }
     }
     p->time++;
+    return cudaSuccess;
+}
+
+// One record pair of the 3-D kernel integral, the plan's current state as the adjoint fields.
+template <typename T>
+cudaError_t kacc3(sparc3d_plan *p, const T *snap, double *out, cudaStream_t st)
+{
+    Plan3<T> &S = plan3<T>(p);
+    const long long F = p->F;
+    cudaError_t e;
+#define K3(call) do { e = (call); if (e != cudaSuccess) return e; } while (0)
+    K3(d3x<T>(p, S.A + 3 * F, S.D1, st));
+    K3(d3y<T>(p, S.A + 4 * F, S.D2, st));
+    K3(d3z<T>(p, S.A + 5 * F, S.D3, 1, st, 1));
+    K3(launch_s3_kacc_div<T>(F, S.D1, S.D2, S.D3, snap, out, st));
+    for (int j = 0; j < 3; j++) {
+        const T *vf = snap + (size_t)(1 + j) * F;
+        K3(d3x<T>(p, vf, S.D1, st));
+        K3(d3y<T>(p, vf, S.D2, st));
+        K3(d3z<T>(p, vf, S.D3, 1, st, 1));
+        K3(launch_s3_kacc_v<T>(F, S.D1, S.D2, S.D3, S.A + (size_t)(3 + j) * F, out, st));
+    }
+#undef K3
     return cudaSuccess;
 }
 
@@ -1773,6 +1837,84 @@ int sparc3d_set_state(sparc3d_plan_t *p, const void *src, void *stream)
     const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
     void *A = p->cfg.precision == 32 ? (void *)p->s32.A : (void *)p->s64.A;
     CK(cudaMemcpyAsync(A, src, 6 * p->F * es, cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)));
+    return SPARC_OK;
+}
+
+int sparc3d_set_adjoint_source(sparc3d_plan_t *p, const double *rows, int nrows, const double *wts, const int *idx,
+                               int ntab, double scale, void *stream)
+{
+    (void)stream;
+    if (!p || !rows || nrows < 1 || !wts || !idx || ntab < 1)
+        return fail(SPARC_ERR_ARG, "sparc3d_set_adjoint_source: bad argument");
+    p->adj = true;
+    p->adj_rows = rows;
+    p->adj_nrows = nrows;
+    p->adj_scale = scale;
+    p->adj_w.assign(wts, wts + (size_t)ntab * 7);
+    p->adj_idx.assign(idx, idx + ntab);
+    return SPARC_OK;
+}
+
+int sparc3d_forward_records(sparc3d_plan_t *p, int nsteps, void *seis, int nrec_cap, int *nrec, void *snaps, int rec0,
+                            int snap_cap, void *stream)
+{
+    if (!p || nsteps < 0 || nrec_cap < 0 || rec0 < 0 || snap_cap < 0 || (snap_cap > 0 && !snaps))
+        return fail(SPARC_ERR_ARG, "sparc3d_forward_records: bad argument");
+    if (!p->have_bg) return fail(SPARC_ERR_STATE, "sparc3d_forward_records: background not set");
+    if (p->cfg.steps_out < 1) return fail(SPARC_ERR_ARG, "sparc3d_forward_records: steps_out must be >= 1");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int n = 0;
+    for (int i = 0; i < nsteps; i++) {
+        cudaError_t e = p->cfg.precision == 32
+                            ? step3<float>(p, (float *)seis, nrec_cap, n, st, (float *)snaps, rec0, snap_cap)
+                            : step3<double>(p, (double *)seis, nrec_cap, n, st, (double *)snaps, rec0, snap_cap);
+        if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("sparc3d_forward_records: ") + cudaGetErrorString(e));
+    }
+    if (nrec) *nrec = n;
+    return SPARC_OK;
+}
+
+int sparc3d_kernels_accumulate(sparc3d_plan_t *p, const void *snaps, int slot, double *out, void *stream)
+{
+    if (!p || !snaps || slot < 0 || !out) return fail(SPARC_ERR_ARG, "sparc3d_kernels_accumulate: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t off = (size_t)slot * 5 * p->F;
+    cudaError_t e = p->cfg.precision == 32 ? kacc3<float>(p, (const float *)snaps + off, out, st)
+                                           : kacc3<double>(p, (const double *)snaps + off, out, st);
+    if (e != cudaSuccess) return fail(SPARC_ERR_CUDA, std::string("sparc3d_kernels_accumulate: ") + cudaGetErrorString(e));
+    return SPARC_OK;
+}
+
+size_t sparc3d_checkpoint_bytes(const sparc3d_plan_t *p)
+{
+    if (!p) return 0;
+    const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
+    return (6 * (size_t)p->F + 2 * (size_t)p->P) * es;
+}
+
+int sparc3d_checkpoint_save(sparc3d_plan_t *p, void *dst, int *time, void *stream)
+{
+    if (!p || !dst || !time) return fail(SPARC_ERR_ARG, "sparc3d_checkpoint_save: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
+    const void *A = p->cfg.precision == 32 ? (const void *)p->s32.A : (const void *)p->s64.A;
+    const void *PV = p->cfg.precision == 32 ? (const void *)p->s32.PV : (const void *)p->s64.PV;
+    CK(cudaMemcpyAsync(dst, A, 6 * p->F * es, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync((char *)dst + 6 * p->F * es, PV, 2 * p->P * es, cudaMemcpyDeviceToDevice, st));
+    *time = p->time;
+    return SPARC_OK;
+}
+
+int sparc3d_checkpoint_load(sparc3d_plan_t *p, const void *src, int time, void *stream)
+{
+    if (!p || !src) return fail(SPARC_ERR_ARG, "sparc3d_checkpoint_load: bad argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t es = p->cfg.precision == 32 ? sizeof(float) : sizeof(double);
+    void *A = p->cfg.precision == 32 ? (void *)p->s32.A : (void *)p->s64.A;
+    void *PV = p->cfg.precision == 32 ? (void *)p->s32.PV : (void *)p->s64.PV;
+    CK(cudaMemcpyAsync(A, src, 6 * p->F * es, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(PV, (const char *)src + 6 * p->F * es, 2 * p->P * es, cudaMemcpyDeviceToDevice, st));
+    p->time = time;
     return SPARC_OK;
 }
 

@@ -429,9 +429,25 @@ cudaError_t launch_s3_div(const S3Args &a, const S3Bg<T> &bg, const T *D1, const
 template <typename T>
 cudaError_t launch_s3_adv(const S3Args &a, const T *D1, const T *D2, const T *D3, const T *V0X, const T *V0Y,
                           const T *V0Z, T *OUT, cudaStream_t st);
+struct S3Lagr {  // the 7 LAGRANGE_INTERP weights of one step
+    double w[7];
+};
 template <typename T>
 cudaError_t launch_s3_rhs(const S3Args &a, const S3Bg<T> &bg, const T *X, T *SCR, const T *GX, const T *GY,
-                          const T *GZ, const T *PSIP, T *SPSIP, const T *RHO, const T *PAT, T amp, cudaStream_t st);
+                          const T *GZ, const T *PSIP, T *SPSIP, const T *RHO, const T *PAT, T amp, const T *ADJ,
+                          int k_obs, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s3_adjsrc(long long lvl, long long nxy, const double *rows, int nrows, int i0, const S3Lagr &w,
+                             double scale, T *ADJ, cudaStream_t st);
+template <typename T>
+cudaError_t launch_s3_record(long long F, const T *D1, const T *D2, const T *D3, const T *A, const T *SCR, T *snap,
+                             cudaStream_t st);
+template <typename T>
+cudaError_t launch_s3_kacc_div(long long F, const T *D1, const T *D2, const T *D3, const T *snap, double *out,
+                               cudaStream_t st);
+template <typename T>
+cudaError_t launch_s3_kacc_v(long long F, const T *D1, const T *D2, const T *D3, const T *va, double *out,
+                             cudaStream_t st);
 template <typename T>
 cudaError_t launch_s3_end(const S3Args &a, T *A, const T *SCR, T dt, int filter, T *PV, const T *SPV,
                           cudaStream_t st);

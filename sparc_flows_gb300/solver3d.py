@@ -146,6 +146,60 @@ class WaveSolver3D:
                    "sparc3d_forward")
         return seis[:min(n.value, cap)]
 
+    @property
+    def adjoint_scale(self) -> float:
+        """delta_width / rho0(o_rad): the factor of the kernel-mode adjoint forcing
+        (displacement.f90:615-627), delta_width = 2 / (z(o_rad+1) - z(o_rad-1))."""
+        k = self.o_rad
+        return 2.0 / (self.z[k + 1] - self.z[k - 1]) / self.profiles["rho0"][k]
+
+    def set_adjoint_source(self, rows: torch.Tensor, wts: np.ndarray, idx: np.ndarray, scale: float | None = None):
+        """Kernel-mode adjoint source: slices rows (nb, nrows, ny, nx) FP64 on the device at the
+        record cadence, LAGRANGE_INTERP table (wts (ntab, 7), idx (ntab,)) per step."""
+        self._adj_rows = rows.to(device=self.dev, dtype=torch.float64).contiguous()  # the plan keeps the pointer
+        self._adj_w = np.ascontiguousarray(wts, dtype=np.float64)
+        self._adj_i = np.ascontiguousarray(idx, dtype=np.int32)
+        capi.check(self.L.sparc3d_set_adjoint_source(
+            self.plan, self._adj_rows.data_ptr(), self._adj_rows.shape[1],
+            self._adj_w.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+            self._adj_i.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(self._adj_i),
+            self.adjoint_scale if scale is None else float(scale), self._stream()), "sparc3d_set_adjoint_source")
+
+    def forward_records(self, nsteps: int, snaps: torch.Tensor | None, rec0: int = 0,
+                        seis: torch.Tensor | None = None) -> int:
+        """nsteps steps; kernel-stage records rec0 .. rec0 + len(snaps) - 1 to snaps
+        (nslot, 5, nz, nb, ny, nx); v_z records of the call to seis if given.  Returns the number of
+        v_z records the call made."""
+        n = ctypes.c_int(0)
+        cap = 0 if seis is None else seis.shape[0]
+        capi.check(self.L.sparc3d_forward_records(
+            self.plan, nsteps, 0 if seis is None else seis.data_ptr(), cap, ctypes.byref(n),
+            0 if snaps is None else snaps.data_ptr(), rec0, 0 if snaps is None else snaps.shape[0], self._stream()),
+            "sparc3d_forward_records")
+        return n.value
+
+    def record_buffer(self, nslot: int) -> torch.Tensor:
+        return torch.zeros((nslot, 5, self.nz, self.nb, self.ny, self.nx), dtype=self.dtype, device=self.dev)
+
+    def kernels_accumulate(self, snaps: torch.Tensor, slot: int, out: torch.Tensor):
+        """Add the kernel integrands of forward record slot of snaps against the current state
+        (the adjoint fields) to out (5, nz, nb, ny, nx) FP64."""
+        capi.check(self.L.sparc3d_kernels_accumulate(self.plan, snaps.data_ptr(), slot, out.data_ptr(), self._stream()),
+                   "sparc3d_kernels_accumulate")
+
+    def checkpoint_bytes(self) -> int:
+        return int(self.L.sparc3d_checkpoint_bytes(self.plan))
+
+    def checkpoint_save(self, buf: torch.Tensor) -> int:
+        t = ctypes.c_int(0)
+        capi.check(self.L.sparc3d_checkpoint_save(self.plan, buf.data_ptr(), ctypes.byref(t), self._stream()),
+                   "sparc3d_checkpoint_save")
+        return t.value
+
+    def checkpoint_load(self, buf: torch.Tensor, time: int):
+        capi.check(self.L.sparc3d_checkpoint_load(self.plan, buf.data_ptr(), int(time), self._stream()),
+                   "sparc3d_checkpoint_load")
+
     def state(self) -> torch.Tensor:
         st = torch.empty((6, self.nz, self.nb, self.ny, self.nx), dtype=self.dtype, device=self.dev)
         capi.check(self.L.sparc3d_get_state(self.plan, st.data_ptr(), self._stream()), "sparc3d_get_state")
