@@ -657,7 +657,7 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP32-vs-FP64 accuracy report")
     ap.add_argument("--no-gradient", action="store_true", help="skip the gradient post-processing figures")
     ap.add_argument("--no-checkpoint", action="store_true", help="skip the checkpointed-run figures")
-    ap.add_argument("--autotune", action="store_true", help="uneven48: time column-pass variants per group first")
+    ap.add_argument("--autotune", action="store_true", help="uneven48: pick each group's column pass first, timed with every group running at once")
     ap.add_argument("--accuracy", action="store_true",
                     help="uneven48: each solve's FP32 error against the same solve in FP64 (one more FP64 run)")
     ap.add_argument("--workload", default="batch32", choices=["batch32", "uneven48", "3d4"],

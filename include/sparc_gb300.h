@@ -61,8 +61,11 @@ typedef struct {
                                   (other values: 32) */
     int column_impl;           /* column pass: 0 partitioned solve with direct loads, 1 partitioned
                                   solve with TMA-staged tiles, 2 (FP32 plans) geometric-band
-                                  inverse of the compact operator with direct loads, 3 (FP32 plans)
-                                  geometric band with TMA-staged tiles; FP64 plans use 0 for 2, 3 */
+                                  inverse of the compact operator with direct loads (32-column
+                                  blocks on nz = 300, nx = 128, 256, 512, 1024: the inputs of its
+                                  first and third phases TMA-staged), 3 (FP32 plans) geometric
+                                  band in 8-column blocks with TMA-staged tiles; FP64 plans use 0
+                                  for 2, 3 */
 } sparc_config_t;
 
 /* Background, all DEVICE pointers to FP64 arrays; copied (and rounded for FP32 plans) into

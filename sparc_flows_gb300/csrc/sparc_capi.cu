@@ -456,8 +456,8 @@ cudaError_t upload_fft(int n, DevFFT<T> &d, std::vector<void *> &allocs)
     return e;
 }
 
-// 2-D tiled tensor map over rows x nx of an x-fastest field array (box: 8 columns x boxr rows).
-bool encode_map(CUtensorMap *m, const void *base, int nx, long long rows, int boxr, size_t esize)
+// 2-D tiled tensor map over rows x nx of an x-fastest field array (box: boxw columns x boxr rows).
+bool encode_map(CUtensorMap *m, const void *base, int nx, long long rows, int boxr, size_t esize, int boxw = 8)
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
@@ -470,7 +470,7 @@ bool encode_map(CUtensorMap *m, const void *base, int nx, long long rows, int bo
     }
     const cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)nx * esize};
-    const cuuint32_t box[2] = {8u, (cuuint32_t)boxr};
+    const cuuint32_t box[2] = {(cuuint32_t)boxw, (cuuint32_t)boxr};
     const cuuint32_t estr[2] = {1u, 1u};
     CUresult r = encode(m, esize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2,
                         const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -484,6 +484,8 @@ struct Solver {
     StepArgs<T> a{};
     ColMaps maps{};
     bool have_maps = false;
+    ColMaps32 maps32{};        // 32-column boxes of nz/2 rows (TMA-staged first phase of the banded pass)
+    bool have_maps32 = false;
     DevZ<T> z[4];
     DevFFT<T> fft;
     BandDev band{};    // banded z-derivative tables (FP32 plans, column_impl 2)
@@ -643,6 +645,11 @@ int alloc_solver(sparc_plan *p)
             for (int d = 0; d < BAND_NPOW; d++) { S.band.rpow[d] = (float)rp; rp *= hb[0].r; }
             S.band_R = R;
             S.band_cw = bcw;
+            // specialised grids: the first phase's inputs staged by TMA (boxes of 32 columns x nz/2 rows)
+            S.have_maps32 = col_band_specialised(nx, nz, bcw, R) && nz % 2 == 0 && nz / 2 <= 256 &&
+                            encode_map(&S.maps32.A, A, nx, (long long)nb * 4 * nz, nz / 2, sizeof(float), 32) &&
+                            encode_map(&S.maps32.SV, SV, nx, (long long)3 * nb * 2 * nz, nz / 2, sizeof(float), 32) &&
+                            encode_map(&S.maps32.DX, DX, nx, (long long)nb * nz, nz / 2, sizeof(float), 32);
         }
     }
     // TMA tiles: boxes of boxr rows, a multiple of 128 bytes so both boxes of a tile start
@@ -695,16 +702,17 @@ cudaError_t col_stage(sparc_plan *p, const StepArgs<T> &a, cudaStream_t st)
             case 13: return launch_col_stage_band_tma<13>(S.maps, a, S.band, st);
             default: break;
         }
+        const ColMaps32 *m32 = S.have_maps32 ? &S.maps32 : nullptr;
         switch (S.band_cw * 100 + S.band_R) {
-            case 3208: return launch_col_stage_band<32, 8>(a, S.band, st);
-            case 3210: return launch_col_stage_band<32, 10>(a, S.band, st);
-            case 3212: return launch_col_stage_band<32, 12>(a, S.band, st);
-            case 1609: return launch_col_stage_band<16, 9>(a, S.band, st);
-            case 1611: return launch_col_stage_band<16, 11>(a, S.band, st);
-            case 1613: return launch_col_stage_band<16, 13>(a, S.band, st);
-            case 809: return launch_col_stage_band<8, 9>(a, S.band, st);
-            case 811: return launch_col_stage_band<8, 11>(a, S.band, st);
-            case 813: return launch_col_stage_band<8, 13>(a, S.band, st);
+            case 3208: return launch_col_stage_band<32, 8>(a, S.band, m32, st);
+            case 3210: return launch_col_stage_band<32, 10>(a, S.band, m32, st);
+            case 3212: return launch_col_stage_band<32, 12>(a, S.band, m32, st);
+            case 1609: return launch_col_stage_band<16, 9>(a, S.band, m32, st);
+            case 1611: return launch_col_stage_band<16, 11>(a, S.band, m32, st);
+            case 1613: return launch_col_stage_band<16, 13>(a, S.band, m32, st);
+            case 809: return launch_col_stage_band<8, 9>(a, S.band, m32, st);
+            case 811: return launch_col_stage_band<8, 11>(a, S.band, m32, st);
+            case 813: return launch_col_stage_band<8, 13>(a, S.band, m32, st);
             default: break;
         }
     }
@@ -1215,6 +1223,8 @@ int sparc_check_state(sparc_plan_t *p, double *norms, void *stream)
     CK(cudaMemcpy(&derr, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (derr == SPARC_DEV_ERR_TMA_TIMEOUT)
         return fail(SPARC_ERR_TIMEOUT, "sparc_check_state: a bounded wait for staged column tiles gave up");
+    if (derr == SPARC_DEV_ERR_TMA_ALIGN)
+        return fail(SPARC_ERR_CUDA, "sparc_check_state: shared memory of the column pass not 128-byte aligned for TMA");
     if (bad) return fail(SPARC_ERR_NONFINITE, "sparc_check_state: non-finite v_z (the solve diverged)");
     return SPARC_OK;
 }
@@ -1231,7 +1241,7 @@ int sparc_plan_describe(const sparc_plan_t *p, char *buf, int len)
                   (col_band_specialised(p->cfg.nx, p->cfg.nz, S.band_cw, S.band_R)
                        ? std::to_string(p->cfg.nx) + "," + std::to_string(p->cfg.nz)
                        : std::string("0,0")) +
-                  ">";
+                  (S.have_maps32 ? ",1>" : ",0>");
         else if (S.have_maps && p->cfg.column_impl == 1) col = "col_stage_tma_kernel<float>";
         else col = "col_stage_kernel<float," + std::to_string(S.a.colw) + ">";
         end = S.a.ALO ? (S.end_stream ? "end_step_comp_kernel" : "end_step_kernel<float>")

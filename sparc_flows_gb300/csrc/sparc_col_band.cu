@@ -7,17 +7,59 @@
 // rows that are R apart; with R odd for CW < 32 they fall on disjoint banks.  Shared memory:
 // two field columns F[nz][CW], two right-hand-side columns [nz][CW], the carries of two
 // derivatives and seven depth profiles.
+//
+// On the specialised grids (TMA1) the first phase's three input tiles (xi_z and v_z of the state,
+// the RHS of v_z two stages back) are staged by 2-D bulk tensor copies into the two RHS tiles and
+// the second field tile, which are idle until phase 2: one thread issues them at kernel start,
+// and the block stages its PML rows and depth profiles while they are in flight.  Once phase 1
+// has read them, the same thread stages phase 3's dxi_x/dx and v_x tiles into the second RHS
+// tile and the second field tile (free until phases 4 and 3), in flight during phase 2.  (The
+// inputs of phases 5 and 7 are L2-prefetched instead: staging them too gained nothing.)
 #include "sparc_band.cuh"
+#include "sparc_tma.cuh"
 
 namespace sparc {
+
+constexpr uint32_t BAND_TMA_WAIT_ITERS = 1u << 24;
+constexpr int BAND_SMEM_PAD = 16;  // the mbarrier after the PML rows (8 bytes, 8-byte aligned)
+
+// Every thread waits (bounded) for the mbarrier phase of parity par, then par flips.  On a
+// time-out anywhere in the block: the error flag is set, the copies are waited for again
+// (bounded) and false is returned to every thread, which then leave the kernel.
+__device__ __forceinline__ bool band_tma_wait(uint64_t *bar, uint32_t &par, int *d_err)
+{
+    const bool ok = mbar_wait_bounded(bar, par, BAND_TMA_WAIT_ITERS);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicExch(d_err, SPARC_DEV_ERR_TMA_TIMEOUT);
+        mbar_wait_bounded(bar, par, BAND_TMA_WAIT_ITERS);
+        __syncthreads();
+        return false;
+    }
+    par ^= 1u;
+    return true;
+}
+
+// One [nz][32] tile (two boxes of nz/2 rows) from rows row0 .. row0 + nz - 1 of map at x0.
+template <int NZ>
+__device__ __forceinline__ void band_tma_tile(float *dst, const CUtensorMap *map, int x0, int row0, uint64_t *bar)
+{
+    tma_load_2d(dst, map, x0, row0, bar);
+    tma_load_2d(dst + (NZ / 2) * 32, map, x0, row0 + NZ / 2, bar);
+}
 
 // NX, NZ: the grid as compile-time constants (0: taken from the arguments).  With them every
 // global and shared-memory offset of the unrolled row loops is an immediate, and with NZ a
 // multiple of R every thread group is full; the generic instantiation serves other grids.
-template <int CW, int R, int NX, int NZ>
-__global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band_kernel(StepArgs<float> a, BandDev bd)
+// TMA1 (CW = 32, even NZ with NZ/2 <= 256): the inputs of phases 1 and 3 staged by TMA through
+// the maps m.
+template <int CW, int R, int NX, int NZ, bool TMA1>
+__global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>())
+    col_band_kernel(StepArgs<float> a, BandDev bd, const __grid_constant__ ColMaps32 m)
 {
-    extern __shared__ __align__(16) float smb[];
+    static_assert(!TMA1 || (CW == 32 && NZ > 0 && NZ % 2 == 0 && NZ / 2 <= 256), "TMA1 geometry");
+    // tiles of nz x 32 floats are nz * 128 bytes long: with a 128-byte aligned base every tile and
+    // half tile is a valid TMA destination
+    extern __shared__ __align__(128) float smb[];
     const int nz = NZ ? NZ : a.nz, nx = NX ? NX : a.nx;
     const int G = blockDim.x / CW;
     const int ncar = 2 * G * CW + BandCarry<CW, R>::floats_fixed();
@@ -33,6 +75,31 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     // (replaced by their new RHS once used), az, bz, fdz
     const int nzp = a.nzpml;
     float *PS = KPB + 7 * nz;
+    // TMA1: the mbarrier, on the first 8-byte boundary after the PML rows
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smb + ((PS - smb + 5 * nzp * CW + 1) & ~1));
+    uint32_t tma_par = 0;  // parity of the mbarrier phase awaited next
+    const int s = a.stage;
+    const int b = blockIdx.y;
+    if constexpr (TMA1) {
+        if ((smem_u32(smb) & 127u) != 0) {  // uniform over the block: no copy is issued
+            if (threadIdx.x == 0) atomicExch(a.d_err, SPARC_DEV_ERR_TMA_ALIGN);
+            return;
+        }
+        // xi_z -> RA, v_z -> RB (s >= 2), RHS of v_z at stage s-2 -> FB (s >= 3), two boxes each
+        if (threadIdx.x == 0) {
+            mbar_init(bar, 1);
+            fence_mbar_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t nt = 1 + (s >= 2 ? 1 : 0) + (s >= 3 ? 1 : 0);
+            mbar_arrive_expect_tx(bar, nt * (uint32_t)NZ * CW * sizeof(float));
+            const int x0 = blockIdx.x * CW;
+            band_tma_tile<NZ>(RA, &m.A, x0, (b * 4 + F_XIZ) * NZ, bar);
+            if (s >= 2) band_tma_tile<NZ>(RB, &m.A, x0, (b * 4 + F_VZ) * NZ, bar);
+            if (s >= 3) band_tma_tile<NZ>(FB, &m.SV, x0, ((a.slot_sm2 * a.nb + b) * 2 + 1) * NZ, bar);
+        }
+    }
     for (int k = threadIdx.x; k < nz; k += blockDim.x) {  // depth profiles
         Kst[k] = __ldg(a.stretch + k);
         Kri[k] = __ldg(a.rhoinv + k);
@@ -44,12 +111,10 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     }
     const int c = threadIdx.x % CW, g = threadIdx.x / CW;
     const int x = blockIdx.x * CW + c;
-    const int b = blockIdx.y;
     const int k0 = g * R;
     const int n = (NZ && NZ % R == 0) ? R : min(R, nz - k0);
     const size_t F = (size_t)nz * nx;
     const float *Ab = a.A + (size_t)b * 4 * F;
-    const int s = a.stage;
     const float bs = a.bs, bsm1 = a.bsm1;
     const int time = *a.d_time;
     const bool xbc = (x == 0 || x == nx - 1);
@@ -82,25 +147,50 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     }
 
     // ---- 1: xi_z at stage s (scr xi_z = v_z of stage s-1 with the RHS boundary zeros)
+    if constexpr (TMA1) {
+        if (!band_tma_wait(bar, tma_par, a.d_err)) return;
+    }
     float xz[R];
 #pragma unroll
     for (int m = 0; m < R; m++) {
         xz[m] = 0.f;
         if (m < n) {
             const int k = k0 + m;
-            const size_t q = (size_t)k * nx + x;
-            float v = __ldg(Ab + F_XIZ * F + q);
-            if (s >= 2) {
-                const float avz = __ldg(Ab + F_VZ * F + q);
-                float t = (s == 2) ? avz : avz + bsm1 * __ldg(svp(a, a.slot_sm2, b, 1) + q);
-                if (k == 0 || xbc) t = 0.f;
-                v += bs * t;
+            float v;
+            if constexpr (TMA1) {
+                v = RA[k * CW + c];
+                if (s >= 2) {
+                    const float avz = RB[k * CW + c];
+                    float t = (s == 2) ? avz : avz + bsm1 * FB[k * CW + c];
+                    if (k == 0 || xbc) t = 0.f;
+                    v += bs * t;
+                }
+            } else {
+                const size_t q = (size_t)k * nx + x;
+                v = __ldg(Ab + F_XIZ * F + q);
+                if (s >= 2) {
+                    const float avz = __ldg(Ab + F_VZ * F + q);
+                    float t = (s == 2) ? avz : avz + bsm1 * __ldg(svp(a, a.slot_sm2, b, 1) + q);
+                    if (k == 0 || xbc) t = 0.f;
+                    v += bs * t;
+                }
             }
             xz[m] = v;
             FA[k * CW + c] = v;
         }
     }
     __syncthreads();
+    if constexpr (TMA1) {
+        // phase 3's tiles: dxi_x/dx -> RB, v_x of the state -> FB: phase 1's generic-proxy reads of both tiles are
+        // ordered before the copies by the barrier above and the proxy fence
+        if (threadIdx.x == 0) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(bar, 2u * NZ * CW * sizeof(float));
+            const int x0 = blockIdx.x * CW;
+            band_tma_tile<NZ>(RB, &m.DX, x0, b * NZ, bar);
+            band_tma_tile<NZ>(FB, &m.A, x0, (b * 4 + F_VX) * NZ, bar);
+        }
+    }
     // L2 prefetch of phase 3's per-point inputs of this thread group's rows (one 128-byte line
     // per array and row, spread over the lanes, no registers held), issued once phase 1's own
     // loads have been served so that they do not compete with them
@@ -111,8 +201,8 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
             if (m >= n) continue;
             const float *p;
             switch (ai) {
-                case 0: p = a.DX + (size_t)b * F; break;
-                case 1: p = Ab + F_VX * F; break;
+                case 0: p = TMA1 ? nullptr : a.DX + (size_t)b * F; break;
+                case 1: p = TMA1 ? nullptr : Ab + F_VX * F; break;
                 case 2: p = s >= 2 ? svp(a, a.slot_sm1, b, 0) : nullptr; break;
                 case 3: p = a.c2d ? a.c2rho0 + (size_t)b * a.bg2 : nullptr; break;
                 default: p = nullptr; break;
@@ -149,6 +239,9 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
     {
         float d[R];
         band_eval<CW, R>(bd, bd.uv[2], C0, c, g, G, k0, n, nz, RA, d);
+        if constexpr (TMA1) {
+            if (!band_tma_wait(bar, tma_par, a.d_err)) return;
+        }
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
@@ -163,14 +256,14 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>()) col_band
                     dzz += ps;
                     fd = PS[(4 * nzp + pi) * CW + c];
                 }
-                const float div = __ldg(a.DX + (size_t)b * F + q) + dzz;
+                const float div = (TMA1 ? RB[k * CW + c] : __ldg(a.DX + (size_t)b * F + q)) + dzz;
                 const float c2r = a.c2d ? __ldg(a.c2rho0 + (size_t)b * a.bg2 + q) : Kc2[k];
                 const float gp = Kgp[k] * fd, gr = Kgr[k] * fd;
                 const float p = -c2r * div - gp * xz[m];
                 const float rho = -Kr0[k] * div - gr * xz[m];
                 xz[m] = rho * Kg[k];
                 FA[k * CW + c] = p;
-                float vx = __ldg(Ab + F_VX * F + q);
+                float vx = TMA1 ? FB[k * CW + c] : __ldg(Ab + F_VX * F + q);
                 if (s >= 2) vx += bs * __ldg(svp(a, a.slot_sm1, b, 0) + q);
                 FB[k * CW + c] = vx;
             }
@@ -308,7 +401,7 @@ static size_t band_smem(int nz, int nzpml)
 {
     const int G = (nz + R - 1) / R;
     return ((size_t)4 * nz * CW + 2 * ((size_t)2 * G * CW + BandCarry<CW, R>::floats_fixed()) + (size_t)7 * nz +
-            (size_t)5 * nzpml * CW) * sizeof(float);
+            (size_t)5 * nzpml * CW) * sizeof(float) + BAND_SMEM_PAD;
 }
 
 size_t col_band_smem_bytes(int nz, int nzpml, int R, int cw)
@@ -327,18 +420,18 @@ size_t col_band_smem_bytes(int nz, int nzpml, int R, int cw)
     }
 }
 
-template <int CW, int R, int NX, int NZ>
-static cudaError_t launch_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st)
+template <int CW, int R, int NX, int NZ, bool TMA1>
+static cudaError_t launch_band(const StepArgs<float> &a, const BandDev &bd, const ColMaps32 &m, cudaStream_t st)
 {
     const int G = (a.nz + R - 1) / R;
     if (G > band_maxg<CW>() || a.nx % CW != 0 || R * G - a.nz >= R) return cudaErrorInvalidValue;
     if ((NX && a.nx != NX) || (NZ && a.nz != NZ)) return cudaErrorInvalidValue;
     const size_t smem = band_smem<CW, R>(a.nz, a.nzpml);
-    cudaError_t e = cudaFuncSetAttribute(col_band_kernel<CW, R, NX, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    auto kern = col_band_kernel<CW, R, NX, NZ, TMA1>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid(a.nx / CW, a.nb);
-    col_band_kernel<CW, R, NX, NZ><<<grid, G * CW, smem, st>>>(a, bd);
+    kern<<<grid, G * CW, smem, st>>>(a, bd, m);
     return cudaGetLastError();
 }
 
@@ -349,25 +442,33 @@ bool col_band_specialised(int nx, int nz, int cw, int R)
     return cw == 32 && R == 10 && nz == 300 && (nx == 128 || nx == 256 || nx == 512 || nx == 1024);
 }
 
+template <int CW, int R, int NX, int NZ>
+static cudaError_t launch_band_sp(const StepArgs<float> &a, const BandDev &bd, const ColMaps32 *m32, cudaStream_t st)
+{
+    if (m32) return launch_band<CW, R, NX, NZ, true>(a, bd, *m32, st);
+    return launch_band<CW, R, NX, NZ, false>(a, bd, ColMaps32{}, st);
+}
+
 template <int CW, int R>
-cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st)
+cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, const ColMaps32 *m32, cudaStream_t st)
 {
     if constexpr (CW == 32 && R == 10) {
         if (a.nz == 300) {
             switch (a.nx) {
-                case 128: return launch_band<32, 10, 128, 300>(a, bd, st);
-                case 256: return launch_band<32, 10, 256, 300>(a, bd, st);
-                case 512: return launch_band<32, 10, 512, 300>(a, bd, st);
-                case 1024: return launch_band<32, 10, 1024, 300>(a, bd, st);
+                case 128: return launch_band_sp<32, 10, 128, 300>(a, bd, m32, st);
+                case 256: return launch_band_sp<32, 10, 256, 300>(a, bd, m32, st);
+                case 512: return launch_band_sp<32, 10, 512, 300>(a, bd, m32, st);
+                case 1024: return launch_band_sp<32, 10, 1024, 300>(a, bd, m32, st);
                 default: break;
             }
         }
     }
-    return launch_band<CW, R, 0, 0>(a, bd, st);
+    return launch_band<CW, R, 0, 0, false>(a, bd, ColMaps32{}, st);
 }
 
-#define SPARC_BAND_INST(cw, r) \
-    template cudaError_t launch_col_stage_band<cw, r>(const StepArgs<float> &, const BandDev &, cudaStream_t);
+#define SPARC_BAND_INST(cw, r)                                                                                    \
+    template cudaError_t launch_col_stage_band<cw, r>(const StepArgs<float> &, const BandDev &, const ColMaps32 *, \
+                                                      cudaStream_t);
 SPARC_BAND_INST(32, 8)
 SPARC_BAND_INST(32, 10)
 SPARC_BAND_INST(32, 12)

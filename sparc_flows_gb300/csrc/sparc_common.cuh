@@ -16,6 +16,7 @@ namespace sparc {
 constexpr int WARP = 32;
 constexpr int MAX_NCH = 24;  // chunks per column (nz <= MAX_NCH * LMAX)
 constexpr int SPARC_DEV_ERR_TMA_TIMEOUT = 1;  // device error flag: a bounded mbarrier wait gave up
+constexpr int SPARC_DEV_ERR_TMA_ALIGN = 2;    // ... a TMA destination in shared memory was not 128-byte aligned
 // Geometric-band form of the compact z-derivative (FP32 column pass): T^{-1} as the inverse of
 // the infinite Toeplitz operator, t0 r^|d|, plus rank-BAND_Q corrections on BAND_KC x BAND_KC
 // corners.  BAND_W: minimum rows of zero padding / depth margin the host checks for.
@@ -480,8 +481,11 @@ cudaError_t launch_s12_rhs(const S5Args &a, const S5Bg<T> &bg, const T *X, T *SC
 template <typename T>
 cudaError_t launch_s5_axpy(long long n, T *Y, const T *X, T a, cudaStream_t st);
 
+struct ColMaps32;
+// m32: tensor maps of A and SV with a 32-column box of nz/2 rows, or null; with them the
+// specialised grids stage the first phase's inputs with TMA
 template <int CW, int R>
-cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, cudaStream_t st);
+cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, const ColMaps32 *m32, cudaStream_t st);
 size_t col_band_smem_bytes(int nz, int nzpml, int R, int cw);
 bool col_band_specialised(int nx, int nz, int cw, int R);  // compiled for this grid
 int col_band_rows(int nz, int cw);  // rows per thread group (0: no banded pass for this depth / width)

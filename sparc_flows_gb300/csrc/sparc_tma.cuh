@@ -84,4 +84,12 @@ struct ColMaps {
     CUtensorMap V0Z;  // as C2R
 };
 
+// Tensor maps of the 32-column banded column pass (box: 32 columns x nz/2 rows): the state A,
+// the RHS ring SV and the row pass's dxi_x/dx, rows as in ColMaps.
+struct ColMaps32 {
+    CUtensorMap A;
+    CUtensorMap SV;
+    CUtensorMap DX;  // rows b*nz + k
+};
+
 }  // namespace sparc

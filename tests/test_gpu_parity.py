@@ -191,7 +191,7 @@ def test_fp32_plans_launch_the_banded_column_pass():
     w = gpu_solver(run, model, psi, cmul, precision=32)
     d = w.describe()
     w.close()
-    assert d["column"].startswith("col_band_kernel<32,10,512,300>"), d
+    assert d["column"].startswith("col_band_kernel<32,10,512,300,1>"), d  # TMA-staged first phase
 
 
 def test_fp32_512_columns_track_fp64():

@@ -101,7 +101,7 @@ def test_nx384_fp32_tracks_fp64():
     specs = [M.SourceSpec(-30.0), M.SourceSpec(45.0)]
     s64, st64, _ = gpu_run(run, model, specs, psi=psi, cmul=cmul)
     s32, st32, desc = gpu_run(run, model, specs, psi=psi, cmul=cmul, precision=32)
-    assert desc["column"].startswith("col_band_kernel<") and desc["column"].endswith(",0,0>"), desc  # generic grid
+    assert desc["column"].startswith("col_band_kernel<") and desc["column"].endswith(",0,0,0>"), desc  # generic grid
     assert rel_l2(s32, s64) < FP32_TOL
     for b in range(2):
         for f in range(4):

@@ -33,15 +33,20 @@ def test_grouped_concurrent_run_equals_single_solves():
         assert np.linalg.norm(ker[i] - kref) <= 1e-6 * np.linalg.norm(kref), i
 
 
-def test_autotuned_groups_pick_a_candidate_and_agree():
-    """Each group's column variant is one of the timed candidates, and its seismograms agree with
-    the default variant's to FP32 accuracy (different variants round differently)."""
+@pytest.mark.parametrize("mode", ["alone", "concurrent"])
+def test_autotuned_groups_pick_a_candidate_and_agree(mode):
+    """Each group's column variant is one of the timed candidates (timed on the group's plan alone,
+    or in rounds of every group at once), and its seismograms agree with the default variant's to
+    FP32 accuracy (different variants round differently)."""
     from sparc_flows_gb300.uneven import COLUMN_CANDIDATES, UnevenBatch
     solves = [M.Solve(256, 60, 100.0, 0.02, -10.0), M.Solve(384, 60, 50.0, 0.01, 0.0)]
-    tuned = UnevenBatch(solves, precision=32, autotune=True)
+    tuned = UnevenBatch(solves, precision=32, autotune=mode)
+    assert len(tuned.tuned) == 2
     for key, t in tuned.tuned.items():
         assert tuple(t["choice"]) in COLUMN_CANDIDATES[32]
-        assert len(t["ms_per_step"]) == len(COLUMN_CANDIDATES[32])
+        assert t["how"] == mode
+        timed = t["ms_per_step"] if mode == "alone" else t["round_s"]
+        assert len(timed) == len(COLUMN_CANDIDATES[32]) and min(timed.values()) > 0
     tuned.run()
     plain = UnevenBatch(solves, precision=32, autotune=False)
     plain.run()
