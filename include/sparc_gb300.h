@@ -62,7 +62,7 @@ typedef struct {
     int column_impl;           /* column pass: 0 partitioned solve with direct loads, 1 partitioned
                                   solve with TMA-staged tiles, 2 (FP32 plans) geometric-band
                                   inverse of the compact operator with direct loads (32-column
-                                  blocks on nz = 300, nx = 128, 256, 512, 1024: the inputs of its
+                                  blocks on nz = 300, nx = 128, 256, 384, 512, 1024: the inputs of its
                                   first and third phases TMA-staged), 3 (FP32 plans) geometric
                                   band in 8-column blocks with TMA-staged tiles; FP64 plans use 0
                                   for 2, 3 */

@@ -436,10 +436,10 @@ static cudaError_t launch_band(const StepArgs<float> &a, const BandDev &bd, cons
 }
 
 // Grids with a compiled specialisation: nz = 300 (the reference's params.i depth) with the
-// 32-column, 10-row geometry and nx = 128 .. 1024.
+// 32-column, 10-row geometry and nx = 128, 256, 384, 512, 1024.
 bool col_band_specialised(int nx, int nz, int cw, int R)
 {
-    return cw == 32 && R == 10 && nz == 300 && (nx == 128 || nx == 256 || nx == 512 || nx == 1024);
+    return cw == 32 && R == 10 && nz == 300 && (nx == 128 || nx == 256 || nx == 384 || nx == 512 || nx == 1024);
 }
 
 template <int CW, int R, int NX, int NZ>
@@ -457,6 +457,7 @@ cudaError_t launch_col_stage_band(const StepArgs<float> &a, const BandDev &bd, c
             switch (a.nx) {
                 case 128: return launch_band_sp<32, 10, 128, 300>(a, bd, m32, st);
                 case 256: return launch_band_sp<32, 10, 256, 300>(a, bd, m32, st);
+                case 384: return launch_band_sp<32, 10, 384, 300>(a, bd, m32, st);
                 case 512: return launch_band_sp<32, 10, 512, 300>(a, bd, m32, st);
                 case 1024: return launch_band_sp<32, 10, 1024, 300>(a, bd, m32, st);
                 default: break;

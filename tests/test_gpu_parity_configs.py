@@ -77,15 +77,15 @@ def test_plain64_full_length_matches_oracle(plain64):
     assert max(errs) < 10 * FP64_TOL, errs
 
 
-def _case384(nsteps):
-    run = M.uneven_run(384, nsteps)
+def _case384(nsteps, nx=384):
+    run = M.uneven_run(nx, nsteps)
     model = M.polytrope(300)
     psi = M.gaussian_psi(run, model, M.psi_amplitude_for_peak(run, model, 240.0))
     return run, model, psi, M.c_bump(run, model)
 
 
 def test_nx384_fp64_matches_oracle():
-    """384 columns: the mixed-radix (3 x 2^7) row FFT and the generic (unspecialised) column pass."""
+    """384 columns: the mixed-radix (3 x 2^7) row FFT and the FP64 partitioned column pass."""
     run, model, psi, cmul = _case384(150)
     spec = M.SourceSpec(20.0)
     seis, st, desc = gpu_run(run, model, [spec], psi=psi, cmul=cmul)
@@ -96,12 +96,14 @@ def test_nx384_fp64_matches_oracle():
         assert rel_l2(st[0, f], a_o[f]) < FP64_TOL, f
 
 
-def test_nx384_fp32_tracks_fp64():
-    run, model, psi, cmul = _case384(300)
+@pytest.mark.parametrize("nx,column", [(384, "col_band_kernel<32,10,384,300,1>"),  # specialised, TMA-staged
+                                       (192, "col_band_kernel<32,10,0,0,0>")])  # generic grid
+def test_fp32_tracks_fp64(nx, column):
+    run, model, psi, cmul = _case384(300, nx)
     specs = [M.SourceSpec(-30.0), M.SourceSpec(45.0)]
     s64, st64, _ = gpu_run(run, model, specs, psi=psi, cmul=cmul)
     s32, st32, desc = gpu_run(run, model, specs, psi=psi, cmul=cmul, precision=32)
-    assert desc["column"].startswith("col_band_kernel<") and desc["column"].endswith(",0,0,0>"), desc  # generic grid
+    assert desc["column"] == column, desc
     assert rel_l2(s32, s64) < FP32_TOL
     for b in range(2):
         for f in range(4):
