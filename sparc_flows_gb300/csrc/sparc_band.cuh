@@ -80,8 +80,9 @@ __device__ __forceinline__ void band_rhs(const ZTab<float> &tb, const float *Fc,
     }
 }
 
-// Carries of the group's right-hand sides and its partial products with the corner factors.
-template <int CW, int R>
+// Carries of the group's right-hand sides and its partial products with the corner factors
+// (TOPC: also the top corner's; not needed where the top block is solved directly, ibc 1 and 2).
+template <int CW, int R, bool TOPC = true>
 __device__ __forceinline__ void band_publish(const BandDev &bd, const float *__restrict__ uv, const BandCarry<CW, R> &cb,
                                              int c, int g, int k0, int n, int nz, const float (&rhs)[R])
 {
@@ -108,7 +109,7 @@ __device__ __forceinline__ void band_publish(const BandDev &bd, const float *__r
         }
     }
     const int o = nz - KC, gt0 = o / R;
-    if (g >= gt0) {
+    if (TOPC && g >= gt0) {
         const float *Vt = uv + 3 * KC * Q;
 #pragma unroll
         for (int q = 0; q < Q; q++) {
@@ -121,12 +122,51 @@ __device__ __forceinline__ void band_publish(const BandDev &bd, const float *__r
     }
 }
 
+// Top block of one column by the direct tridiagonal solve (for ibc 1 and 2 the boundary row of
+// T is not diagonally dominant and T^{-1} reaches 19 there, which a product with T^{-1} carries
+// into FP32 rounding): x at row o-1 (outside the corner block) from the band sums over 27 rows
+// on either side, then the Thomas sweeps over rows o .. nz-1 into y[0 .. KC) (stride CW).  Rc
+// and y never overlap (right-hand-side tile, workspace): with the restrict qualifiers the loads
+// of Rc are issued ahead of the stores to y instead of waiting behind each of them on the
+// sweep's dependency chain.
+template <int CW, int THT>
+__device__ __forceinline__ void band_thomas(const BandDev &bd, const float *__restrict__ Rc, float *__restrict__ y,
+                                            int c, int nz)
+{
+    constexpr int KC = BAND_KC;
+    const int o = nz - KC;
+    const float *th = bd.th[THT];
+    const int m0 = o - 1;
+    float lo = 0.f, up = 0.f;
+#pragma unroll
+    for (int d = 27; d >= 1; d--)
+        if (m0 - d >= 0) lo = fmaf(bd.rpow[d], Rc[(m0 - d) * CW + c], lo);
+#pragma unroll
+    for (int d = KC; d >= 1; d--) up = fmaf(bd.rpow[d], Rc[(m0 + d) * CW + c], up);
+    const float xm0 = bd.t0 * (Rc[m0 * CW + c] + lo + up);
+    float prev = 0.f;
+#pragma unroll
+    for (int m = 0; m < KC; m++) {
+        float v = Rc[(o + m) * CW + c];
+        if (m == 0) v = fmaf(-th[3 * KC], xm0, v);
+        v = v * th[m];
+        if (m > 0) v = fmaf(-th[KC + m], prev, v);
+        y[m * CW] = v;
+        prev = v;
+    }
+#pragma unroll
+    for (int m = KC - 2; m >= 0; m--) {
+        prev = fmaf(-th[2 * KC + m + 1], prev, y[m * CW]);
+        y[m * CW] = prev;
+    }
+}
+
 // x[m] = (T^{-1} rhs)[k0 + m] for m < n, from the group's own right-hand sides (column Rc) and
-// the carries.
-template <int CW, int R>
+// the carries.  THT = 0, 1: the top block by the direct solve with the Thomas factors of ibc 1, 2
+// (-1: by the corner factors).
+template <int CW, int R, int THT = -1>
 __device__ __forceinline__ void band_eval(const BandDev &bd, const float *__restrict__ uv, const BandCarry<CW, R> &cb,
-                                          int c, int g, int G, int k0, int n, int nz, const float *Rc, float (&x)[R],
-                                          bool thomas_top = false)
+                                          int c, int g, int G, int k0, int n, int nz, const float *Rc, float (&x)[R])
 {
     constexpr int KC = BAND_KC, Q = BAND_Q;
     float rhs[R];
@@ -173,34 +213,9 @@ __device__ __forceinline__ void band_eval(const BandDev &bd, const float *__rest
         }
     }
     const int o = nz - KC, gt0 = o / R;
-    if (k0 + n > o && thomas_top) {
-        // Top block by a direct tridiagonal solve: for ibc 1 and 2 the boundary row of T is not
-        // diagonally dominant and T^{-1} reaches 19 there, which a product with T^{-1} carries
-        // into FP32 rounding.  x at row o-1 (outside the corner block) from the band sums over
-        // 27 rows on either side, then the chunk-local Thomas sweeps over rows o .. nz-1.
-        const float *th = uv + 4 * KC * Q;
-        const int m0 = o - 1;
-        float lo = 0.f, up = 0.f;
-#pragma unroll
-        for (int d = 27; d >= 1; d--)
-            if (m0 - d >= 0) lo = fmaf(bd.rpow[d], Rc[(m0 - d) * CW + c], lo);
-#pragma unroll
-        for (int d = KC; d >= 1; d--) up = fmaf(bd.rpow[d], Rc[(m0 + d) * CW + c], up);
-        const float xm0 = bd.t0 * (Rc[m0 * CW + c] + lo + up);
+    if (THT >= 0 && k0 + n > o) {
         float *y = cb.YT + (size_t)(g - gt0) * KC * CW + c;  // this group's column of the scratch
-        float prev = 0.f;
-        for (int m = 0; m < KC; m++) {
-            float v = Rc[(o + m) * CW + c];
-            if (m == 0) v = fmaf(-th[3 * KC], xm0, v);
-            v = v * __ldg(th + m);
-            if (m > 0) v = fmaf(-__ldg(th + KC + m), prev, v);
-            y[m * CW] = v;
-            prev = v;
-        }
-        for (int m = KC - 2; m >= 0; m--) {
-            prev = fmaf(-__ldg(th + 2 * KC + m + 1), prev, y[m * CW]);
-            y[m * CW] = prev;
-        }
+        band_thomas<CW, THT < 0 ? 0 : THT>(bd, Rc, y, c, nz);
 #pragma unroll
         for (int r = 0; r < R; r++)
             if (r < n && k0 + r >= o) x[r] = y[(k0 + r - o) * CW];

@@ -639,6 +639,9 @@ int alloc_solver(sparc_plan *p)
             S.band.uv[i] = (const float *)ptr;
         }
         if (ok) {
+            for (int i = 0; i < 2; i++)  // Thomas factors of ibc 1, 2 as kernel-parameter copies
+                for (int j = 0; j < 3 * BAND_KC + 1; j++)
+                    S.band.th[i][j] = (float)hb[i].uv[(size_t)4 * BAND_KC * BAND_Q + j];
             S.band.t0 = (float)hb[0].t0;
             S.band.r = (float)hb[0].r;
             double rp = 1.0;

@@ -274,12 +274,12 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>())
     {
         float rr[R];
         band_rhs<CW, R>(a.z2, FA, RA, c, k0, n, nz, 0.f, rr);
-        band_publish<CW, R>(bd, bd.uv[1], C0, c, g, k0, n, nz, rr);
+        band_publish<CW, R, false>(bd, bd.uv[1], C0, c, g, k0, n, nz, rr);
     }
     if (a.flows) {
         float rr[R];
         band_rhs<CW, R>(a.z1, FB, RB, c, k0, n, nz, 0.f, rr);
-        band_publish<CW, R>(bd, bd.uv[0], C1, c, g, k0, n, nz, rr);
+        band_publish<CW, R, false>(bd, bd.uv[0], C1, c, g, k0, n, nz, rr);
     }
 #pragma unroll
     for (int m = 0; m < R; m++)
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>())
     // v_x kept in FB); v_z of stage s
     {
         float d[R];
-        band_eval<CW, R>(bd, bd.uv[1], C0, c, g, G, k0, n, nz, RA, d, true);
+        band_eval<CW, R, 1>(bd, bd.uv[1], C0, c, g, G, k0, n, nz, RA, d);
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>())
                 xz[m] = -Kri[k] * (gpz + xz[m]);
             }
         }
-        if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C1, c, g, G, k0, n, nz, RB, d, true);
+        if (a.flows) band_eval<CW, R, 0>(bd, bd.uv[0], C1, c, g, G, k0, n, nz, RB, d);
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
@@ -332,12 +332,12 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>())
     if (a.flows) {
         float rr[R];
         band_rhs<CW, R>(a.z1, FA, RA, c, k0, n, nz, 0.f, rr);
-        band_publish<CW, R>(bd, bd.uv[0], C0, c, g, k0, n, nz, rr);
+        band_publish<CW, R, false>(bd, bd.uv[0], C0, c, g, k0, n, nz, rr);
         __syncthreads();
     }
     // ---- 7: finish RHS v_z (advection, source, boundary zeros); this stage's stores
     float d[R];
-    if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C0, c, g, G, k0, n, nz, RA, d, true);
+    if (a.flows) band_eval<CW, R, 0>(bd, bd.uv[0], C0, c, g, G, k0, n, nz, RA, d);
     float forcing = 0.f;
     const bool inject = (time <= a.src_until) && (time >= 0) && (time < a.ntab);
     if (inject && a.k_inj >= k0 && a.k_inj < k0 + n) {

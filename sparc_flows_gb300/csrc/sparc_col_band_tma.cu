@@ -196,18 +196,18 @@ __global__ void __launch_bounds__(BT_CW * 32, 2)
     {
         float rr[R];
         band_rhs<CW, R>(a.z2, B3, RA, c, k0, n, nz, 0.f, rr);
-        band_publish<CW, R>(bd, bd.uv[1], C0, c, g, k0, n, nz, rr);
+        band_publish<CW, R, false>(bd, bd.uv[1], C0, c, g, k0, n, nz, rr);
     }
     if (a.flows) {
         float rr[R];
         band_rhs<CW, R>(a.z1, B5, RB, c, k0, n, nz, 0.f, rr);
-        band_publish<CW, R>(bd, bd.uv[0], C1, c, g, k0, n, nz, rr);
+        band_publish<CW, R, false>(bd, bd.uv[0], C1, c, g, k0, n, nz, rr);
     }
     if (!bt_phase(bar, 2) || !bt_phase(bar, 3)) { bt_abort(bar, 5, a.d_err); return; }
     // ---- 5: gradient of p, RHS v_z without advection; advection of v_x along z; v_z of stage s
     {
         float d[R];
-        band_eval<CW, R>(bd, bd.uv[1], C0, c, g, G, k0, n, nz, RA, d, true);
+        band_eval<CW, R, 1>(bd, bd.uv[1], C0, c, g, G, k0, n, nz, RA, d);
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(BT_CW * 32, 2)
                 xz[m] = -Kri[k] * (gpz + xz[m]);
             }
         }
-        if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C1, c, g, G, k0, n, nz, RB, d, true);
+        if (a.flows) band_eval<CW, R, 0>(bd, bd.uv[0], C1, c, g, G, k0, n, nz, RB, d);
 #pragma unroll
         for (int m = 0; m < R; m++) {
             if (m < n) {
@@ -245,12 +245,12 @@ __global__ void __launch_bounds__(BT_CW * 32, 2)
     if (a.flows) {
         float rr[R];
         band_rhs<CW, R>(a.z1, B1, RA, c, k0, n, nz, 0.f, rr);
-        band_publish<CW, R>(bd, bd.uv[0], C0, c, g, k0, n, nz, rr);
+        band_publish<CW, R, false>(bd, bd.uv[0], C0, c, g, k0, n, nz, rr);
     }
     if (!bt_phase(bar, 4)) { bt_abort(bar, 5, a.d_err); return; }
     // ---- 7: finish RHS v_z (advection, source, boundary zeros)
     float d[R];
-    if (a.flows) band_eval<CW, R>(bd, bd.uv[0], C0, c, g, G, k0, n, nz, RA, d, true);
+    if (a.flows) band_eval<CW, R, 0>(bd, bd.uv[0], C0, c, g, G, k0, n, nz, RA, d);
     float forcing = 0.f;
     const bool inject = (time <= a.src_until) && (time >= 0) && (time < a.ntab);
     if (inject && a.k_inj >= k0 && a.k_inj < k0 + n) {

@@ -101,6 +101,11 @@ struct BandDev {
     float t0, r;
     float rpow[BAND_NPOW];
     const float *uv[3];
+    // Thomas factors of the top block for ibc 1 and 2 (copies of uv[0], uv[1] from 4 KC Q on:
+    // 1/beta, lower/beta, gamma, the coupling to row nz-KC-1): indexed with compile-time
+    // offsets, they are constant-bank operands of the sweeps' arithmetic, with no load on the
+    // recurrence's chain
+    float th[2][3 * BAND_KC + 1];
 };
 
 
