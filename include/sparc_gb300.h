@@ -167,7 +167,10 @@ int sparc_check_state(sparc_plan_t *plan, double *norms, void *stream);
 int sparc_get_time(sparc_plan_t *plan, int *time, void *stream);
 
 /* Diagnostics (no counterpart in the reference): the kernels this plan launches for its column
- * and end-of-step passes, as "column=<kernel> end=<kernel>" (NUL-terminated, at most len bytes). */
+ * and end-of-step passes and whether each row pass starts on the SMs the column pass's last wave
+ * leaves idle, as "column=<kernel> end=<kernel> stage_overlap=<0|1>" (NUL-terminated, at most len
+ * bytes).  The overlap is on for FP32 plans of 512 columns with the banded column pass unless
+ * SPARC_STAGE_OVERLAP=0 is set when the plan is created. */
 int sparc_plan_describe(const sparc_plan_t *plan, char *buf, int len);
 
 /* Kernel construction from paired snapshots (kernels.f90:209-358): for record pair

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -684,6 +685,24 @@ int alloc_solver(sparc_plan *p)
                 S.band_tma_R = Rt;
         }
     }
+    // stage overlap: the 512-column row pass starts on the SMs that the banded column pass's last
+    // wave leaves idle, each row block waiting for its own solve's column tiles only
+    // (SPARC_STAGE_OVERLAP=0 turns it off)
+    a.tile_cnt = nullptr;
+    a.tiles_per_solve = 0;
+    {
+        const char *ov = std::getenv("SPARC_STAGE_OVERLAP");
+        const bool want = !(ov && ov[0] == '0');
+        if (want && sizeof(T) == 4 && nx == 512 && S.band_R > 0 && S.band_tma_R == 0 && c.column_impl == 2) {
+            void *ptr = nullptr;
+            if (cudaMalloc(&ptr, (size_t)5 * nb * sizeof(int)) != cudaSuccess)
+                return fail(SPARC_ERR_CUDA, "cudaMalloc: stage-overlap counters");
+            S.allocs.push_back(ptr);
+            cudaMemset(ptr, 0, (size_t)5 * nb * sizeof(int));
+            a.tile_cnt = (int *)ptr;
+            a.tiles_per_solve = nx / S.band_cw;
+        }
+    }
     return SPARC_OK;
 }
 
@@ -741,6 +760,7 @@ cudaError_t enqueue_step(sparc_plan *p, StepArgs<T> a, cudaStream_t st)
 {
     const double *B = p->cfg.betas;  // B[s-1] = beta of stage s (B[0] = 0)
     cudaError_t e;
+    if (a.tile_cnt && (e = cudaMemsetAsync(a.tile_cnt, 0, (size_t)5 * a.nb * sizeof(int), st)) != cudaSuccess) return e;
     for (int s = 1; s <= 5; s++) {
         a.stage = s;
         a.bs = (T)B[s - 1];
@@ -778,6 +798,7 @@ int profile_passes(sparc_plan *p, int nsteps, double *ms, cudaStream_t st)
     };
     cudaError_t e = cudaSuccess;
     for (int i = 0; i < nsteps && e == cudaSuccess; i++) {
+        if (a.tile_cnt) e = cudaMemsetAsync(a.tile_cnt, 0, (size_t)5 * a.nb * sizeof(int), st);
         for (int s = 1; s <= 5 && e == cudaSuccess; s++) {
             a.stage = s; a.bs = (T)B[s - 1]; a.bsm1 = (s >= 2) ? (T)B[s - 2] : T(0);
             a.slot_s = s % 3; a.slot_sm1 = (s - 1) % 3; a.slot_sm2 = (s + 1) % 3;
@@ -1226,6 +1247,8 @@ int sparc_check_state(sparc_plan_t *p, double *norms, void *stream)
     CK(cudaMemcpy(&derr, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (derr == SPARC_DEV_ERR_TMA_TIMEOUT)
         return fail(SPARC_ERR_TIMEOUT, "sparc_check_state: a bounded wait for staged column tiles gave up");
+    if (derr == SPARC_DEV_ERR_STAGE_WAIT)
+        return fail(SPARC_ERR_TIMEOUT, "sparc_check_state: a row pass gave up waiting for its solve's column tiles");
     if (derr == SPARC_DEV_ERR_TMA_ALIGN)
         return fail(SPARC_ERR_CUDA, "sparc_check_state: shared memory of the column pass not 128-byte aligned for TMA");
     if (bad) return fail(SPARC_ERR_NONFINITE, "sparc_check_state: non-finite v_z (the solve diverged)");
@@ -1257,7 +1280,8 @@ int sparc_plan_describe(const sparc_plan_t *p, char *buf, int len)
         end = (S.have_maps && p->cfg.column_impl == 1) ? "end_step_tma_kernel<double>"
               : S.end_stream ? "end_step_stream_kernel<double>" : "end_step_kernel<double>";
     }
-    const std::string d = "column=" + col + " end=" + end;
+    const bool overlap = p->cfg.precision == 32 && p->s32.a.tile_cnt != nullptr;
+    const std::string d = "column=" + col + " end=" + end + " stage_overlap=" + (overlap ? "1" : "0");
     std::snprintf(buf, (size_t)len, "%s", d.c_str());
     return SPARC_OK;
 }

@@ -80,6 +80,9 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>())
     uint32_t tma_par = 0;  // parity of the mbarrier phase awaited next
     const int s = a.stage;
     const int b = blockIdx.y;
+    // stage overlap: every block has started once all have passed this point, so the row pass
+    // launched as this grid's dependent takes only SMs that no block of this grid still needs
+    if (a.tile_cnt) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if constexpr (TMA1) {
         if ((smem_u32(smb) & 127u) != 0) {  // uniform over the block: no copy is issued
             if (threadIdx.x == 0) atomicExch(a.d_err, SPARC_DEV_ERR_TMA_ALIGN);
@@ -380,6 +383,13 @@ __global__ void __launch_bounds__(CW *band_maxg<CW>(), band_minb<CW>())
         const int pi = i / CW, cc = i - pi * CW;
         a.SPZ[a.slot_s * spz_slot + ((size_t)b * 2 * nzp + pi + nzp) * nx + blockIdx.x * CW + cc] =
             PS[(1 * nzp + pi) * CW + cc];
+    }
+    if (a.tile_cnt) {  // this tile of solve b is done: its stores, then the count (release)
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(a.tile_cnt + (size_t)(s - 1) * a.nb + b, 1);
+        }
     }
 }
 

@@ -17,6 +17,7 @@ constexpr int WARP = 32;
 constexpr int MAX_NCH = 24;  // chunks per column (nz <= MAX_NCH * LMAX)
 constexpr int SPARC_DEV_ERR_TMA_TIMEOUT = 1;  // device error flag: a bounded mbarrier wait gave up
 constexpr int SPARC_DEV_ERR_TMA_ALIGN = 2;    // ... a TMA destination in shared memory was not 128-byte aligned
+constexpr int SPARC_DEV_ERR_STAGE_WAIT = 3;   // ... a row pass gave up waiting for its solve's column tiles
 // Geometric-band form of the compact z-derivative (FP32 column pass): T^{-1} as the inverse of
 // the infinite Toeplitz operator, t0 r^|d|, plus rank-BAND_Q corrections on BAND_KC x BAND_KC
 // corners.  BAND_W: minimum rows of zero padding / depth margin the host checks for.
@@ -66,6 +67,13 @@ struct StepArgs {
     int colw;                // column-pass block width (8 or 32 columns)
     int boxr;                // rows per TMA box of the staged column pass (2 boxes cover nz)
     int *d_err;              // device error flag (SPARC_DEV_ERR_*)
+    // stage overlap (FP32 banded column pass followed by the 512-column row pass): tile_cnt[s-1][b]
+    // counts the column tiles of solve b finished in stage s (tiles_per_solve when complete); the
+    // row pass of stage s+1, launched as a programmatic dependent of the column pass, starts on
+    // SMs the column pass's last wave leaves idle and waits for its own solve's count only.
+    // nullptr: no overlap
+    int *tile_cnt;
+    int tiles_per_solve;
     const T *inj_scale, *src_rows;
     int nrows;
     const double *src_w;

@@ -250,11 +250,45 @@ __device__ __forceinline__ void row_mid_store_pml(const StepArgs<float> &a, cons
 // FP32 rows of 512 columns: the same row pass with the register-resident FFT (sparc_fft512.cuh);
 // register n2 of a lane holds column lane + 32 n2.  Each part loads everything it needs before it
 // stores anything, so no load waits behind a store of the row it may alias.
+constexpr uint32_t STAGE_WAIT_ITERS = 1u << 21;  // polls of 128 ns: about 0.3 s
+
+// Stage overlap: wait (bounded) until every column tile of the solves of this block's rows is
+// done.  Thread 0 polls with acquire loads; the barrier passes what it saw to the block.  Returns
+// false to every thread on a time-out, with the device error flag set (and at once once that
+// flag is set).
+__device__ __forceinline__ bool stage_wait(const StepArgs<float> &a, int row0, int nrows)
+{
+    bool ok = true;
+    if (threadIdx.x == 0) {
+        // once any device error is flagged (a wait that gave up, a column block that left early)
+        // the waits of the rest fail at once
+        if (*(volatile int *)a.d_err != 0) ok = false;
+        const int last = min(row0 + nrows, a.nb * a.nz) - 1;
+        const int *cnt = a.tile_cnt + (size_t)(a.stage - 2) * a.nb;
+        for (int b = row0 / a.nz; ok && b <= last / a.nz; b++) {
+            uint32_t it = 0;
+            for (;;) {
+                int v;
+                asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(cnt + b) : "memory");
+                if (v >= a.tiles_per_solve) break;
+                if (++it > STAGE_WAIT_ITERS) {
+                    ok = false;
+                    break;
+                }
+                __nanosleep(128);
+            }
+        }
+        if (!ok) atomicExch(a.d_err, SPARC_DEV_ERR_STAGE_WAIT);
+    }
+    return !__syncthreads_or(!ok);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(ROW_WPB *WARP, 4) row_stage_reg512_kernel(StepArgs<float> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (MODE != 0 && a.tile_cnt && !stage_wait(a, blockIdx.x * ROW_WPB, ROW_WPB)) return;
     if (MODE == 0 && blockIdx.x == 0 && threadIdx.x == 0) *a.d_time += 1;  // new step begins
     const int row = blockIdx.x * ROW_WPB + warp;
     if (row >= a.nb * a.nz) return;
@@ -364,6 +398,20 @@ template <int MODE>
 static void row_reg512_launch(const StepArgs<float> &a, int grid, cudaStream_t st)
 {
     const size_t smem = (size_t)ROW_WPB * FFT512_SCRATCH * sizeof(float);
+    if (MODE != 0 && a.tile_cnt) {  // a programmatic dependent of the column pass before it
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(ROW_WPB * WARP);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, row_stage_reg512_kernel<MODE>, a);
+        return;
+    }
     row_stage_reg512_kernel<MODE><<<grid, ROW_WPB * WARP, smem, st>>>(a);
 }
 

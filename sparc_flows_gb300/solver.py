@@ -409,7 +409,8 @@ class WaveSolver:
     LAUNCHES_PER_STEP = 12  # 6 row passes, 5 column passes, 1 end-of-step pass
 
     def describe(self) -> dict:
-        """Kernels of the column and end-of-step passes of this plan (sparc_plan_describe)."""
+        """Kernels of the column and end-of-step passes of this plan and whether the row pass
+        overlaps the column pass's last wave (sparc_plan_describe)."""
         buf = ctypes.create_string_buffer(256)
         capi.check(self.L.sparc_plan_describe(self.plan, buf, 256), "sparc_plan_describe")
         return dict(kv.split("=", 1) for kv in buf.value.decode().split())

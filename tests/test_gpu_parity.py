@@ -192,6 +192,26 @@ def test_fp32_plans_launch_the_banded_column_pass():
     d = w.describe()
     w.close()
     assert d["column"].startswith("col_band_kernel<32,10,512,300,1>"), d  # TMA-staged first phase
+    assert d["stage_overlap"] == "1", d
+
+
+def test_stage_overlap_is_bit_identical(monkeypatch):
+    """The row pass started on the SMs the column pass's last wave leaves idle, each row block
+    waiting for its own solve's column tiles, gives the same bits as the serialised step: state
+    and seismograms of 60 steps of four solves, with and without the overlap."""
+    run, model, psi, cmul = make_case(nx=512, nsteps=60, length=400e8)
+    out = {}
+    for ov in ("0", "1"):
+        monkeypatch.setenv("SPARC_STAGE_OVERLAP", ov)
+        w = gpu_solver(run, model, psi, cmul, nb=4, precision=32)
+        assert w.describe()["stage_overlap"] == ov
+        w.set_forward_sources([M.SourceSpec(x) for x in (-40.0, -10.0, 15.0, 50.0)])
+        seis = w.forward().cpu().numpy()
+        out[ov] = (seis, w.state().cpu().numpy())
+        w.check()
+        w.close()
+    assert np.abs(out["0"][0]).max() > 0
+    assert np.array_equal(out["0"][0], out["1"][0]) and np.array_equal(out["0"][1], out["1"][1])
 
 
 def test_fp32_512_columns_track_fp64():
