@@ -785,6 +785,7 @@ int profile_passes(sparc_plan *p, int nsteps, double *ms, cudaStream_t st)
     StepArgs<T> a = solver<T>(p).a;
     a.fsign = T(1);
     a.seis = nullptr; a.snaps = nullptr; a.nrec_cap = 0;
+    a.tile_cnt = nullptr;  // passes timed one by one: no stage overlap, whose row pass would wait
     a.unstretch_top = (T)p->unstretch_top;
     const double *B = p->cfg.betas;
     std::vector<cudaEvent_t> ev;
@@ -798,7 +799,6 @@ int profile_passes(sparc_plan *p, int nsteps, double *ms, cudaStream_t st)
     };
     cudaError_t e = cudaSuccess;
     for (int i = 0; i < nsteps && e == cudaSuccess; i++) {
-        if (a.tile_cnt) e = cudaMemsetAsync(a.tile_cnt, 0, (size_t)5 * a.nb * sizeof(int), st);
         for (int s = 1; s <= 5 && e == cudaSuccess; s++) {
             a.stage = s; a.bs = (T)B[s - 1]; a.bsm1 = (s >= 2) ? (T)B[s - 2] : T(0);
             a.slot_s = s % 3; a.slot_sm1 = (s - 1) % 3; a.slot_sm2 = (s + 1) % 3;
