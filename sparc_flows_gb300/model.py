@@ -203,7 +203,7 @@ def lagrange_weights(run: RunConfig, nsteps: int, num_steps: int, nsrc_rows: int
 
 
 # --------------------------------------------------------------------------------------
-# The BASELINE workloads
+# Benchmark workloads (FP64 plain run, autograd run, source batch)
 # --------------------------------------------------------------------------------------
 def workload(name: str):
     """Return (RunConfig, model, list[SourceSpec], psi or None, cmul or None) for a workload.
